@@ -1,0 +1,183 @@
+/*
+ * rsc.h -- GB300 (sm_103a) backend for SimRadar's per-pulse emulation loop.
+ *
+ * This is the C ABI that the RS framework host (rs.c) calls in place of its
+ * OpenCL calls.  One rsc_worker owns the device state of one RSWorker
+ * (rs.h:150-266): the scatterer attribute arrays, the lookup tables and the
+ * pulse.  Every entry point names the rs.c code it replaces.  Plain pointers
+ * and sizes only; every function returns RSC_OK (0) or a negative status and
+ * never exits the process.  rsc_last_error() returns the message of the last
+ * failure on the calling thread.
+ *
+ * Data layout (identical to the reference host arrays, rs.h:304-313):
+ *   attribute arrays are float4 / uint4 per scatterer (16 B, x fastest):
+ *     pos (x, y, z, radius)  vel (u, v, w, -)  ori, tum (quaternion x, y, z, w)
+ *     aux (range, age, dsd bin, angular weight)  rcs, sig (Ih, Qh, Iv, Qv)
+ *     rnd (4 x 32-bit seeds)
+ *   images are float4 arrays, x fastest (CL_RGBA / CL_FLOAT, rs.c:2857).
+ *   descriptors are the float[16] / float[4] vectors the kernels receive
+ *   (sim_desc: rs_enum.h:93-110, table descriptors: rs_enum.h:10-91).
+ */
+#ifndef SIMRADAR_GB300_RSC_H
+#define SIMRADAR_GB300_RSC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSC_OK 0
+#define RSC_ERR_ARG (-1)        /* invalid argument (NULL, size, index) */
+#define RSC_ERR_CUDA (-2)       /* a CUDA runtime call failed */
+#define RSC_ERR_NOMEM (-3)      /* device or pinned host allocation failed */
+#define RSC_ERR_STATE (-4)      /* call out of order (e.g. before rsc_worker_malloc) */
+#define RSC_ERR_UNSUPPORTED (-5) /* a table or mode the kernels do not handle */
+
+#define RSC_MAX_TYPES 8         /* RS_MAX_DEBRIS_TYPES, rs_const.h:24 */
+#define RSC_MAX_GATES 512       /* RS_MAX_GATES, rs_const.h:22 */
+
+/* pulse-formation precision (additive; the reference has only RSC_PULSE_PLAIN) */
+#define RSC_PULSE_PLAIN 0       /* FP32 exactly as rs.cl scat_sig_aux + pass 1 (gate weights bit-exact) */
+#define RSC_PULSE_COMPENSATED 1 /* FP32 with split range phase, FP64 gate origins, compensated sums */
+#define RSC_PULSE_F64 2         /* FP64 reference of the same FP32 state (error metric oracle) */
+
+typedef struct rsc_worker rsc_worker;
+
+/* Population layout of one worker: type 0 is the background (rain), types
+ * 1..RSC_MAX_TYPES-1 are debris; counts[k] scatterers start at origins[k]
+ * (RSWorker.origins / .counts, rs.h:160-161, set by RS_update_origins_offsets
+ * rs.c:2259-2359).  Debris type k uses ADM table adm_index[k] and RCS table
+ * rcs_index[k] (the round-robin a / r indices of rs.c:5351-5373). */
+typedef struct {
+    uint64_t origins[RSC_MAX_TYPES];
+    uint64_t counts[RSC_MAX_TYPES];
+    int32_t adm_index[RSC_MAX_TYPES];
+    int32_t rcs_index[RSC_MAX_TYPES];
+} rsc_population;
+
+/* Last error message of this thread (never NULL). */
+const char *rsc_last_error(void);
+
+/* Number of visible CUDA devices (replaces get_device_info, rs.c:95-223). */
+int rsc_device_count(int *count);
+
+/* Create a worker on a device: stream, events and the kernels' launch
+ * configuration.  Replaces RS_worker_init's context / queue / program /
+ * kernel creation (rs.c:383-545). */
+int rsc_worker_create(int device, rsc_worker **out);
+
+/* Release every device allocation of the worker.  Replaces RS_worker_free
+ * (rs.c:547-621) and the device half of RS_free_scat_memory (rs.c:1182-1246). */
+int rsc_worker_free(rsc_worker *w);
+
+/* Allocate the attribute arrays for num_scats scatterers (padded to a multiple
+ * of 64, the padding zeroed) and the pulse for range_count gates starting at
+ * range_start every range_delta.  aux, rcs and sig start at zero.  Replaces
+ * RS_worker_malloc (rs.c:623-944): its clCreateBuffer calls, the zero fill of
+ * aux / rcs / sig and the pass-1 gate arguments (rs.c:872-884). */
+int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float range_delta,
+                      uint32_t range_count);
+
+/* Range weight table W[n] with descriptor (scale, origin, max, user) --
+ * RS_set_range_weight, rs.c:2548-2618. */
+int rsc_set_range_weight(rsc_worker *w, const float *table, uint32_t n, const float desc[4]);
+
+/* Angular weight table -- RS_set_angular_weight, rs.c:2626-2699. */
+int rsc_set_angular_weight(rsc_worker *w, const float *table, uint32_t n, const float desc[4]);
+
+/* Ellipsoid (drop) RCS table of n float4 -- RS_set_rcs_ellipsoid_table,
+ * rs.c:2472-2546. */
+int rsc_set_rcs_ellipsoid(rsc_worker *w, const float *table4, uint32_t n, const float desc[4]);
+
+/* Upload one LES volume (uvwt and cpxx, nx*ny*nz float4 each) into buffer
+ * slot 0 or 1 of the double buffer, and set the LES descriptor.  Replaces the
+ * clCreateImage / clEnqueueWriteImage / descriptor code of RS_set_vel_data
+ * (rs.c:2854-2978).  Synchronous, like the reference (clWaitForEvents,
+ * rs.c:2940).  The dimensions must not change between slots. */
+int rsc_set_les(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx,
+                uint32_t ny, uint32_t nz, const float desc[16]);
+
+/* Same upload, asynchronous: the copy is ordered before the next advance on
+ * the worker's stream, so the caller may refill `slot` while the current one
+ * is in use.  The host buffers must stay valid until rsc_synchronize(). */
+int rsc_set_les_async(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx,
+                      uint32_t ny, uint32_t nz, const float desc[16]);
+
+/* ADM table `index` (drag cd and moment cm images, nx = beta, ny = alpha) --
+ * RS_set_adm_data, rs.c:3642-3763.  index < RSC_MAX_TYPES. */
+int rsc_set_adm(rsc_worker *w, int index, const float *cd4, const float *cm4, uint32_t nx, uint32_t ny,
+                const float desc[16]);
+
+/* RCS table `index` (real and imaginary images, nx = alpha, ny = beta) --
+ * RS_set_rcs_data, rs.c:3852-3973. */
+int rsc_set_rcs(rsc_worker *w, int index, const float *real4, const float *imag4, uint32_t nx, uint32_t ny,
+                const float desc[16]);
+
+/* Debris-flux-field inverse CDF of n floats into slot 0 or 1, and its
+ * descriptor -- RS_set_debris_flux_field_by_icdf, rs.c:3328-3408. */
+int rsc_set_dff(rsc_worker *w, int slot, const float *icdf, uint32_t n, const float desc[16]);
+
+/* Host -> device copy of scatterers [offset, offset + count) of each array
+ * given (NULL skips an array) -- RS_upload, rs.c:5124-5176. */
+int rsc_upload(rsc_worker *w, size_t offset, size_t count, const float *pos4, const float *vel4,
+               const float *ori4, const float *tum4, const float *aux4, const float *rcs4, const float *sig4,
+               const uint32_t *rnd4);
+
+/* Device -> host copy, same convention -- RS_download (rs.c:4961-5016),
+ * RS_download_position_only (rs.c:5018-5040), RS_download_orientation_only
+ * (rs.c:5042-5064).  aux and sig are formed for the latest pulse first if the
+ * pulse kernel did not write them. */
+int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float *vel4, float *ori4,
+                 float *tum4, float *aux4, float *rcs4, float *sig4, uint32_t *rnd4);
+
+/* One time step of every scatterer: the el_atts / bg_atts / fp_atts launch on
+ * type 0 (chosen by the concept bits in sim_desc[5], rs.c:5339-5349) and the
+ * db_atts launch for each debris type (rs.c:5350-5374), in one kernel launch,
+ * reading LES slot les_id.  Replaces the launches and the wait of
+ * RS_advance_time (rs.c:5325-5388).  Asynchronous unless the caller
+ * synchronises; rsc_download / rsc_download_pulse synchronise. */
+int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const float sim_desc[16]);
+
+/* Debris RCS refresh after a beam move: db_rcs for every debris type
+ * (rs.c:5528-5562). */
+int rsc_update_debris_rcs(rsc_worker *w, const rsc_population *pop, const float sim_desc[16]);
+
+/* Form the pulse of the current state for the beam in sim_desc[0..2]:
+ * scat_sig_aux + make_pulse_pass_1 + make_pulse_pass_2 (rs.c:5563-5573) as
+ * one kernel.  The per-gate float4 (Ih, Qh, Iv, Qv) sums stay on the device. */
+int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]);
+
+/* Copy the pulse to host memory (range_count float4) and multiply by `gain`
+ * -- RS_download_pulse_only + RS_merge_pulse_tmp for one worker
+ * (rs.c:5096-5122, rs.c:5066-5094).  Waits for the pulse. */
+int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain);
+
+/* Wait for all work queued on the worker (clFinish). */
+int rsc_synchronize(rsc_worker *w);
+
+/* Pulse-formation precision, RSC_PULSE_* (additive, default PLAIN). */
+int rsc_set_pulse_precision(rsc_worker *w, int mode);
+
+/* Write aux and sig on every pulse (as the reference does) instead of forming
+ * them on download.  Default 0. */
+int rsc_set_materialize_sig_aux(rsc_worker *w, int enable);
+
+/* Number of kernel launches this worker has issued (for accounting). */
+int rsc_launch_count(rsc_worker *w, uint64_t *count);
+
+/* The CUDA stream the worker issues on (as a void pointer, for callers that
+ * time with events on it). */
+int rsc_get_stream(rsc_worker *w, void **stream);
+
+/* Diagnostics: evaluate the shared elementary functions (rsmath.h) on the
+ * device; fn: 0 sin, 1 cos, 2 log, 3 log1p, 4 acos, 5 atan2(a, b), 6 exp,
+ * 7 pow(a, b).  Host arrays of n floats. */
+int rsc_eval_math(int fn, const float *a, const float *b, float *out, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,762 @@
+/*
+ * rsc.cu -- host side of the GB300 backend: the C ABI declared in
+ * include/rsc.h.  Device memory, table uploads, launch geometry and the
+ * lazily formed aux / sig arrays live here; the kernels are in
+ * rsc_kernels.cuh.  Compiled with -fmad=false (see rsmath.h).
+ */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/rsc.h"
+#include "rsc_kernels.cuh"
+
+using rsc::AdvanceArgs;
+using rsc::DebrisType;
+using rsc::Image;
+using rsc::PulseArgs;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define RSC_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            return fail(e_ == cudaErrorMemoryAllocation ? RSC_ERR_NOMEM : RSC_ERR_CUDA,         \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                       \
+    } while (0)
+
+struct Table2D {
+    float4 *a = nullptr, *b = nullptr;
+    uint32_t nx = 0, ny = 0;
+    float desc[16] = {0};
+};
+
+}  // namespace
+
+struct rsc_worker {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    /* attribute arrays */
+    size_t num_scats = 0, numel = 0;
+    float4 *pos = nullptr, *vel = nullptr, *ori = nullptr, *tum = nullptr;
+    float4 *aux = nullptr, *rcs = nullptr, *sig = nullptr;
+    uint4 *rnd = nullptr;
+    /* pulse */
+    uint32_t G = 0;
+    float range_start = 0.0f, range_delta = 0.0f;
+    float4 *pulse = nullptr;
+    double *pulse64 = nullptr;
+    float *rk = nullptr, *rk_hi = nullptr, *rk_lo = nullptr;
+    double *rk64 = nullptr;
+    void *partials = nullptr;
+    size_t partials_bytes = 0;
+    unsigned *counter = nullptr;
+    /* tables */
+    float *range_weight = nullptr;
+    uint32_t range_n = 0;
+    float range_desc[4] = {0};
+    float range_weight_host0 = 1.0f, range_weight_hostm = 1.0f; /* edge values W[0], W[xm] */
+    float *angular_weight = nullptr;
+    uint32_t angular_n = 0;
+    float angular_desc[4] = {0};
+    float4 *ellipsoid = nullptr;
+    uint32_t ellipsoid_n = 0;
+    float ellipsoid_desc[4] = {0};
+    float4 *les_uvwt[2] = {nullptr, nullptr}, *les_cpxx[2] = {nullptr, nullptr};
+    uint32_t les_nx = 0, les_ny = 0, les_nz = 0;
+    float les_desc[16] = {0};
+    Table2D adm[RSC_MAX_TYPES];
+    Table2D rcs_tab[RSC_MAX_TYPES];
+    float *dff[2] = {nullptr, nullptr};
+    uint32_t dff_n = 0;
+    float dff_desc[16] = {0};
+    /* modes and bookkeeping */
+    int precision = RSC_PULSE_PLAIN;
+    int materialize = 0;
+    bool sig_aux_stale = false;
+    bool have_pulse_desc = false;
+    float last_sim[16] = {0};
+    uint64_t launches = 0;
+};
+
+namespace {
+
+int check_worker(rsc_worker *w) {
+    if (w == nullptr) return fail(RSC_ERR_ARG, "worker is NULL");
+    cudaError_t e = cudaSetDevice(w->device);
+    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "cudaSetDevice(%d): %s", w->device, cudaGetErrorString(e));
+    return RSC_OK;
+}
+
+int check_alloc(rsc_worker *w) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (w->pos == nullptr) return fail(RSC_ERR_STATE, "rsc_worker_malloc has not been called");
+    return RSC_OK;
+}
+
+void free_ptr(void *p) {
+    if (p) cudaFree(p);
+}
+
+void free_arrays(rsc_worker *w) {
+    free_ptr(w->pos);
+    free_ptr(w->vel);
+    free_ptr(w->ori);
+    free_ptr(w->tum);
+    free_ptr(w->aux);
+    free_ptr(w->rcs);
+    free_ptr(w->sig);
+    free_ptr(w->rnd);
+    free_ptr(w->pulse);
+    free_ptr(w->pulse64);
+    free_ptr(w->rk);
+    free_ptr(w->rk_hi);
+    free_ptr(w->rk_lo);
+    free_ptr(w->rk64);
+    free_ptr(w->partials);
+    free_ptr(w->counter);
+    w->pos = w->vel = w->ori = w->tum = w->aux = w->rcs = w->sig = w->pulse = nullptr;
+    w->rnd = nullptr;
+    w->pulse64 = nullptr;
+    w->rk = w->rk_hi = w->rk_lo = nullptr;
+    w->rk64 = nullptr;
+    w->partials = nullptr;
+    w->counter = nullptr;
+    w->num_scats = w->numel = 0;
+}
+
+int upload_floats(float **dst, const float *src, size_t n) {
+    free_ptr(*dst);
+    *dst = nullptr;
+    RSC_CUDA(cudaMalloc((void **)dst, n * sizeof(float)));
+    RSC_CUDA(cudaMemcpy(*dst, src, n * sizeof(float), cudaMemcpyHostToDevice));
+    return RSC_OK;
+}
+
+int upload_float4(float4 **dst, const float *src4, size_t n) {
+    free_ptr(*dst);
+    *dst = nullptr;
+    RSC_CUDA(cudaMalloc((void **)dst, n * sizeof(float4)));
+    RSC_CUDA(cudaMemcpy(*dst, src4, n * sizeof(float4), cudaMemcpyHostToDevice));
+    return RSC_OK;
+}
+
+Image make_image(const float4 *d, uint32_t nx, uint32_t ny, uint32_t nz) {
+    Image im;
+    im.data = d;
+    im.nx = (int)nx;
+    im.ny = (int)ny;
+    im.nz = (int)nz;
+    return im;
+}
+
+/* Debris launch description shared by k_advance and k_db_rcs. */
+int fill_debris(rsc_worker *w, const rsc_population *pop, AdvanceArgs &a, unsigned long long *total) {
+    a.ntypes = 0;
+    unsigned long long acc = 0;
+    for (int k = 1; k < RSC_MAX_TYPES; k++) {
+        if (pop->counts[k] == 0) continue;
+        if (pop->origins[k] + pop->counts[k] > w->num_scats) {
+            return fail(RSC_ERR_ARG, "debris type %d range [%llu, %llu) exceeds %zu scatterers", k,
+                        (unsigned long long)pop->origins[k], (unsigned long long)(pop->origins[k] + pop->counts[k]),
+                        w->num_scats);
+        }
+        int ai = pop->adm_index[k], ri = pop->rcs_index[k];
+        if (ai < 0 || ai >= RSC_MAX_TYPES || w->adm[ai].a == nullptr) {
+            return fail(RSC_ERR_STATE, "debris type %d: ADM table %d not set", k, ai);
+        }
+        if (ri < 0 || ri >= RSC_MAX_TYPES || w->rcs_tab[ri].a == nullptr) {
+            return fail(RSC_ERR_STATE, "debris type %d: RCS table %d not set", k, ri);
+        }
+        DebrisType &T = a.types[a.ntypes];
+        T.origin = pop->origins[k];
+        T.count = pop->counts[k];
+        T.cd = make_image(w->adm[ai].a, w->adm[ai].nx, w->adm[ai].ny, 1);
+        T.cm = make_image(w->adm[ai].b, w->adm[ai].nx, w->adm[ai].ny, 1);
+        T.re = make_image(w->rcs_tab[ri].a, w->rcs_tab[ri].nx, w->rcs_tab[ri].ny, 1);
+        T.im = make_image(w->rcs_tab[ri].b, w->rcs_tab[ri].nx, w->rcs_tab[ri].ny, 1);
+        memcpy(T.adm, w->adm[ai].desc, sizeof(T.adm));
+        memcpy(T.rcs, w->rcs_tab[ri].desc, sizeof(T.rcs));
+        a.deb_prefix[a.ntypes] = acc;
+        acc += pop->counts[k];
+        a.ntypes++;
+    }
+    a.deb_prefix[a.ntypes] = acc;
+    *total = acc;
+    return RSC_OK;
+}
+
+/* Gate origins: the FP32 running sum of make_pulse_pass_1 (rs.cl:1214) and
+ * the FP64 values range_start + k * range_delta (head and tail). */
+int set_gates(rsc_worker *w) {
+    const uint32_t G = w->G;
+    std::vector<float> rk(G), hi(G), lo(G);
+    std::vector<double> r64(G);
+    float r = w->range_start;
+    for (uint32_t k = 0; k < G; k++) {
+        rk[k] = r;
+        r = r + w->range_delta;
+        double e = (double)w->range_start + (double)k * (double)w->range_delta;
+        r64[k] = e;
+        hi[k] = (float)e;
+        lo[k] = (float)(e - (double)hi[k]);
+    }
+    RSC_CUDA(cudaMemcpy(w->rk, rk.data(), G * sizeof(float), cudaMemcpyHostToDevice));
+    RSC_CUDA(cudaMemcpy(w->rk_hi, hi.data(), G * sizeof(float), cudaMemcpyHostToDevice));
+    RSC_CUDA(cudaMemcpy(w->rk_lo, lo.data(), G * sizeof(float), cudaMemcpyHostToDevice));
+    RSC_CUDA(cudaMemcpy(w->rk64, r64.data(), G * sizeof(double), cudaMemcpyHostToDevice));
+    return RSC_OK;
+}
+
+int pulse_geometry(rsc_worker *w, int mode, int *grid, int *threads, size_t *smem) {
+    size_t bin_bytes = (mode == RSC_PULSE_PLAIN) ? 16 : 32;  /* per gate per warp */
+    size_t per_warp = (size_t)w->G * bin_bytes;
+    size_t budget = 200 * 1024;
+    int warps = (int)(budget / per_warp);
+    if (warps > 16) warps = 16;
+    if (warps < 1) return fail(RSC_ERR_UNSUPPORTED, "%u gates do not fit the pulse kernel's shared memory", w->G);
+    *threads = warps * 32;
+    *smem = (size_t)warps * per_warp + 2 * w->G * sizeof(float);
+    int per_sm = 1;
+    cudaError_t e;
+    if (mode == RSC_PULSE_PLAIN) {
+        e = cudaFuncSetAttribute(rsc::k_pulse<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<0>, *threads, *smem);
+    } else if (mode == RSC_PULSE_COMPENSATED) {
+        e = cudaFuncSetAttribute(rsc::k_pulse<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<1>, *threads, *smem);
+    } else {
+        e = cudaFuncSetAttribute(rsc::k_pulse<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<2>, *threads, *smem);
+    }
+    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "pulse kernel configuration: %s", cudaGetErrorString(e));
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 4) per_sm = 4;
+    *grid = w->num_sms * per_sm;
+    return RSC_OK;
+}
+
+void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
+    memset(&P, 0, sizeof(P));
+    P.pos = w->pos;
+    P.rcs = w->rcs;
+    P.aux = w->aux;
+    P.sig = w->sig;
+    P.n = w->num_scats;
+    P.aw = w->angular_weight;
+    memcpy(P.awd, w->angular_desc, sizeof(P.awd));
+    P.rw = w->range_weight;
+    memcpy(P.rwd, w->range_desc, sizeof(P.rwd));
+    P.rk = w->rk;
+    P.rk_lo = w->rk_lo;
+    P.rk64 = w->rk64;
+    P.G = w->G;
+    memcpy(P.sim, sim, sizeof(P.sim));
+    P.rs = w->range_start;
+    P.inv_delta = w->range_delta != 0.0f ? 1.0f / w->range_delta : 0.0f;
+    P.partials = w->partials;
+    P.counter = w->counter;
+    P.pulse = w->pulse;
+    P.pulse64 = w->pulse64;
+    /* Candidate window of the sparse path.  The weight is W[0] or W[xm] when
+     * the table index clamps, so when both edge values are 0 only gates with
+     * 0 < (r - r_k) * xs + x0 < xm can receive a non-zero weight; the window is
+     * that interval in gate units plus a margin for the FP32 running sum of
+     * the gate origins and the rounding of the window arithmetic. */
+    P.dense = 1;
+    const float xs = w->range_desc[0], x0 = w->range_desc[1], xm = w->range_desc[2];
+    if (w->range_delta > 0.0f && xs > 0.0f && xm >= 0.0f && w->range_n > 0) {
+        uint32_t im = (uint32_t)xm;
+        if (im < w->range_n && w->range_weight_host0 == 0.0f && w->range_weight_hostm == 0.0f) {
+            double d_lo = -(double)x0 / (double)xs;
+            double d_hi = ((double)xm - (double)x0) / (double)xs;
+            double drift = 0.0, r = w->range_start;
+            float rf = w->range_start;
+            for (uint32_t k = 0; k < w->G; k++) {
+                drift = fmax(drift, fabs((double)rf - r));
+                rf = rf + w->range_delta;
+                r += (double)w->range_delta;
+            }
+            double margin = (drift + 1.0e-3 * fabs((double)w->range_delta)) / (double)w->range_delta + 0.05;
+            double lo = d_lo / (double)w->range_delta - margin;
+            double hi = d_hi / (double)w->range_delta + margin;
+            if (hi - lo + 1.0 < (double)rsc::kMaxCandidates) {
+                P.dense = 0;
+                P.win_lo = (float)lo;
+                P.win_hi = (float)hi;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rsc_last_error(void) { return g_err; }
+
+int rsc_device_count(int *count) {
+    if (count == nullptr) return fail(RSC_ERR_ARG, "count is NULL");
+    int n = 0;
+    RSC_CUDA(cudaGetDeviceCount(&n));
+    *count = n;
+    return RSC_OK;
+}
+
+int rsc_worker_create(int device, rsc_worker **out) {
+    if (out == nullptr) return fail(RSC_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    RSC_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(RSC_ERR_ARG, "device %d of %d", device, n);
+    RSC_CUDA(cudaSetDevice(device));
+    rsc_worker *w = new rsc_worker();
+    w->device = device;
+    cudaError_t e = cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete w;
+        return fail(RSC_ERR_CUDA, "worker creation: %s", cudaGetErrorString(e));
+    }
+    *out = w;
+    return RSC_OK;
+}
+
+int rsc_worker_free(rsc_worker *w) {
+    if (w == nullptr) return RSC_OK;
+    cudaSetDevice(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    free_arrays(w);
+    free_ptr(w->range_weight);
+    free_ptr(w->angular_weight);
+    free_ptr(w->ellipsoid);
+    for (int s = 0; s < 2; s++) {
+        free_ptr(w->les_uvwt[s]);
+        free_ptr(w->les_cpxx[s]);
+        free_ptr(w->dff[s]);
+    }
+    for (int t = 0; t < RSC_MAX_TYPES; t++) {
+        free_ptr(w->adm[t].a);
+        free_ptr(w->adm[t].b);
+        free_ptr(w->rcs_tab[t].a);
+        free_ptr(w->rcs_tab[t].b);
+    }
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return RSC_OK;
+}
+
+int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float range_delta, uint32_t range_count) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (num_scats == 0) return fail(RSC_ERR_ARG, "num_scats is 0");
+    if (range_count == 0 || range_count > RSC_MAX_GATES) {
+        return fail(RSC_ERR_ARG, "range_count %u outside [1, %d]", range_count, RSC_MAX_GATES);
+    }
+    if (!(fabsf(range_start) < INFINITY) || !(fabsf(range_delta) < INFINITY)) {
+        return fail(RSC_ERR_ARG, "range_start / range_delta not finite");
+    }
+    cudaStreamSynchronize(w->stream);
+    free_arrays(w);
+    const size_t numel = (num_scats + 63) / 64 * 64;
+    const size_t b4 = numel * sizeof(float4);
+    w->num_scats = num_scats;
+    w->numel = numel;
+    w->G = range_count;
+    w->range_start = range_start;
+    w->range_delta = range_delta;
+    float4 **arrays[] = {&w->pos, &w->vel, &w->ori, &w->tum, &w->aux, &w->rcs, &w->sig};
+    for (float4 **a : arrays) {
+        cudaError_t e = cudaMalloc((void **)a, b4);
+        if (e != cudaSuccess) {
+            free_arrays(w);
+            return fail(RSC_ERR_NOMEM, "cudaMalloc of %zu B: %s", b4, cudaGetErrorString(e));
+        }
+        RSC_CUDA(cudaMemsetAsync(*a, 0, b4, w->stream));
+    }
+    RSC_CUDA(cudaMalloc((void **)&w->rnd, numel * sizeof(uint4)));
+    RSC_CUDA(cudaMemsetAsync(w->rnd, 0, numel * sizeof(uint4), w->stream));
+    RSC_CUDA(cudaMalloc((void **)&w->pulse, range_count * sizeof(float4)));
+    RSC_CUDA(cudaMemsetAsync(w->pulse, 0, range_count * sizeof(float4), w->stream));
+    RSC_CUDA(cudaMalloc((void **)&w->pulse64, range_count * 4 * sizeof(double)));
+    RSC_CUDA(cudaMalloc((void **)&w->rk, range_count * sizeof(float)));
+    RSC_CUDA(cudaMalloc((void **)&w->rk_hi, range_count * sizeof(float)));
+    RSC_CUDA(cudaMalloc((void **)&w->rk_lo, range_count * sizeof(float)));
+    RSC_CUDA(cudaMalloc((void **)&w->rk64, range_count * sizeof(double)));
+    /* block partials for the largest grid any precision uses (8 B per word) */
+    w->partials_bytes = (size_t)w->num_sms * 4 * range_count * 4 * 8;
+    RSC_CUDA(cudaMalloc(&w->partials, w->partials_bytes));
+    RSC_CUDA(cudaMalloc((void **)&w->counter, sizeof(unsigned)));
+    RSC_CUDA(cudaMemsetAsync(w->counter, 0, sizeof(unsigned), w->stream));
+    s = set_gates(w);
+    if (s) return s;
+    RSC_CUDA(cudaStreamSynchronize(w->stream));
+    w->sig_aux_stale = false;
+    w->have_pulse_desc = false;
+    return RSC_OK;
+}
+
+int rsc_set_range_weight(rsc_worker *w, const float *table, uint32_t n, const float desc[4]) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (table == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "range weight table");
+    if (!(desc[2] >= 0.0f) || (uint32_t)desc[2] >= n) return fail(RSC_ERR_ARG, "range weight max index %g >= %u", desc[2], n);
+    cudaStreamSynchronize(w->stream);
+    s = upload_floats(&w->range_weight, table, n);
+    if (s) return s;
+    w->range_n = n;
+    memcpy(w->range_desc, desc, sizeof(w->range_desc));
+    w->range_weight_host0 = table[0];
+    w->range_weight_hostm = table[(uint32_t)desc[2]];
+    return RSC_OK;
+}
+
+int rsc_set_angular_weight(rsc_worker *w, const float *table, uint32_t n, const float desc[4]) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (table == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "angular weight table");
+    if (!(desc[2] >= 0.0f) || (uint32_t)desc[2] >= n) return fail(RSC_ERR_ARG, "angular weight max index %g >= %u", desc[2], n);
+    cudaStreamSynchronize(w->stream);
+    s = upload_floats(&w->angular_weight, table, n);
+    if (s) return s;
+    w->angular_n = n;
+    memcpy(w->angular_desc, desc, sizeof(w->angular_desc));
+    return RSC_OK;
+}
+
+int rsc_set_rcs_ellipsoid(rsc_worker *w, const float *table4, uint32_t n, const float desc[4]) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (table4 == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "ellipsoid RCS table");
+    if (!(desc[2] >= 0.0f) || (uint32_t)desc[2] >= n) return fail(RSC_ERR_ARG, "ellipsoid max index %g >= %u", desc[2], n);
+    cudaStreamSynchronize(w->stream);
+    s = upload_float4(&w->ellipsoid, table4, n);
+    if (s) return s;
+    w->ellipsoid_n = n;
+    memcpy(w->ellipsoid_desc, desc, sizeof(w->ellipsoid_desc));
+    return RSC_OK;
+}
+
+static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny,
+                        uint32_t nz, const float desc[16], bool async) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
+    if (uvwt4 == nullptr || desc == nullptr || nx == 0 || ny == 0 || nz == 0) return fail(RSC_ERR_ARG, "LES table");
+    const size_t nn = (size_t)nx * ny * nz;
+    if (w->les_uvwt[0] != nullptr && (nx != w->les_nx || ny != w->les_ny || nz != w->les_nz)) {
+        /* new dimensions: reallocate both slots (rs.c:3000-3016 releases them) */
+        cudaStreamSynchronize(w->stream);
+        for (int k = 0; k < 2; k++) {
+            free_ptr(w->les_uvwt[k]);
+            free_ptr(w->les_cpxx[k]);
+            w->les_uvwt[k] = w->les_cpxx[k] = nullptr;
+        }
+    }
+    if (w->les_uvwt[0] == nullptr) {
+        for (int k = 0; k < 2; k++) {
+            RSC_CUDA(cudaMalloc((void **)&w->les_uvwt[k], nn * sizeof(float4)));
+            RSC_CUDA(cudaMalloc((void **)&w->les_cpxx[k], nn * sizeof(float4)));
+            RSC_CUDA(cudaMemsetAsync(w->les_cpxx[k], 0, nn * sizeof(float4), w->stream));
+        }
+        w->les_nx = nx;
+        w->les_ny = ny;
+        w->les_nz = nz;
+    }
+    RSC_CUDA(cudaMemcpyAsync(w->les_uvwt[slot], uvwt4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
+    if (cpxx4) {
+        RSC_CUDA(cudaMemcpyAsync(w->les_cpxx[slot], cpxx4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
+    }
+    memcpy(w->les_desc, desc, sizeof(w->les_desc));
+    if (!async) RSC_CUDA(cudaStreamSynchronize(w->stream));
+    return RSC_OK;
+}
+
+int rsc_set_les(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny, uint32_t nz,
+                const float desc[16]) {
+    return set_les_impl(w, slot, uvwt4, cpxx4, nx, ny, nz, desc, false);
+}
+
+int rsc_set_les_async(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny,
+                      uint32_t nz, const float desc[16]) {
+    return set_les_impl(w, slot, uvwt4, cpxx4, nx, ny, nz, desc, true);
+}
+
+static int set_table2d(rsc_worker *w, Table2D *t, const float *a4, const float *b4, uint32_t nx, uint32_t ny,
+                       const float desc[16]) {
+    if (a4 == nullptr || b4 == nullptr || desc == nullptr || nx == 0 || ny == 0) return fail(RSC_ERR_ARG, "2-D table");
+    cudaStreamSynchronize(w->stream);
+    const size_t nn = (size_t)nx * ny;
+    int s = upload_float4(&t->a, a4, nn);
+    if (s) return s;
+    s = upload_float4(&t->b, b4, nn);
+    if (s) return s;
+    t->nx = nx;
+    t->ny = ny;
+    memcpy(t->desc, desc, sizeof(t->desc));
+    return RSC_OK;
+}
+
+int rsc_set_adm(rsc_worker *w, int index, const float *cd4, const float *cm4, uint32_t nx, uint32_t ny,
+                const float desc[16]) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (index < 0 || index >= RSC_MAX_TYPES) return fail(RSC_ERR_ARG, "ADM index %d", index);
+    return set_table2d(w, &w->adm[index], cd4, cm4, nx, ny, desc);
+}
+
+int rsc_set_rcs(rsc_worker *w, int index, const float *real4, const float *imag4, uint32_t nx, uint32_t ny,
+                const float desc[16]) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (index < 0 || index >= RSC_MAX_TYPES) return fail(RSC_ERR_ARG, "RCS index %d", index);
+    return set_table2d(w, &w->rcs_tab[index], real4, imag4, nx, ny, desc);
+}
+
+int rsc_set_dff(rsc_worker *w, int slot, const float *icdf, uint32_t n, const float desc[16]) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (slot < 0 || slot > 1 || icdf == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "DFF table");
+    /* db_atts reads icdf[floor(clamp(r * sf + {0, 1}, 0, sf))] (rs.cl:799-805) */
+    if (!(desc[15] >= 0.0f) || (uint32_t)desc[15] >= n) return fail(RSC_ERR_ARG, "DFF max index %g >= %u", desc[15], n);
+    cudaStreamSynchronize(w->stream);
+    s = upload_floats(&w->dff[slot], icdf, n);
+    if (s) return s;
+    w->dff_n = n;
+    memcpy(w->dff_desc, desc, sizeof(w->dff_desc));
+    return RSC_OK;
+}
+
+int rsc_upload(rsc_worker *w, size_t offset, size_t count, const float *pos4, const float *vel4, const float *ori4,
+               const float *tum4, const float *aux4, const float *rcs4, const float *sig4, const uint32_t *rnd4) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "upload [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
+    const size_t b = count * 16;
+    struct { void *dst; const void *src; } m[] = {
+        {w->pos + offset, pos4}, {w->vel + offset, vel4}, {w->ori + offset, ori4}, {w->tum + offset, tum4},
+        {w->aux + offset, aux4}, {w->rcs + offset, rcs4}, {w->sig + offset, sig4}, {w->rnd + offset, rnd4}};
+    for (auto &e : m) {
+        if (e.src) RSC_CUDA(cudaMemcpyAsync(e.dst, e.src, b, cudaMemcpyHostToDevice, w->stream));
+    }
+    RSC_CUDA(cudaStreamSynchronize(w->stream));
+    if (aux4 || sig4) w->sig_aux_stale = false;
+    return RSC_OK;
+}
+
+int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float *vel4, float *ori4, float *tum4,
+                 float *aux4, float *rcs4, float *sig4, uint32_t *rnd4) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "download [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
+    if ((aux4 || sig4) && w->sig_aux_stale && w->have_pulse_desc) {
+        PulseArgs P;
+        fill_pulse_args(w, P, w->last_sim);
+        unsigned blocks = (unsigned)((w->num_scats + 255) / 256);
+        rsc::k_sig_aux<<<blocks, 256, 0, w->stream>>>(P);
+        RSC_CUDA(cudaGetLastError());
+        w->launches++;
+        w->sig_aux_stale = false;
+    }
+    const size_t b = count * 16;
+    struct { void *dst; const void *src; } m[] = {
+        {pos4, w->pos + offset}, {vel4, w->vel + offset}, {ori4, w->ori + offset}, {tum4, w->tum + offset},
+        {aux4, w->aux + offset}, {rcs4, w->rcs + offset}, {sig4, w->sig + offset}, {rnd4, w->rnd + offset}};
+    for (auto &e : m) {
+        if (e.dst) RSC_CUDA(cudaMemcpyAsync(e.dst, e.src, b, cudaMemcpyDeviceToHost, w->stream));
+    }
+    RSC_CUDA(cudaStreamSynchronize(w->stream));
+    return RSC_OK;
+}
+
+int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const float sim_desc[16]) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (pop == nullptr || sim_desc == nullptr) return fail(RSC_ERR_ARG, "population / sim_desc is NULL");
+    if (les_id < 0 || les_id > 1 || w->les_uvwt[les_id] == nullptr) return fail(RSC_ERR_STATE, "LES slot %d not set", les_id);
+    if (pop->origins[0] + pop->counts[0] > w->num_scats) return fail(RSC_ERR_ARG, "background range beyond the arrays");
+    const uint32_t concept = rsm_f2u(sim_desc[5]);
+    AdvanceArgs a;
+    memset(&a, 0, sizeof(a));
+    a.pos = w->pos;
+    a.vel = w->vel;
+    a.ori = w->ori;
+    a.tum = w->tum;
+    a.rcs = w->rcs;
+    a.rnd = w->rnd;
+    a.uvwt = make_image(w->les_uvwt[les_id], w->les_nx, w->les_ny, w->les_nz);
+    a.cpxx = make_image(w->les_cpxx[les_id], w->les_nx, w->les_ny, w->les_nz);
+    memcpy(a.wind, w->les_desc, sizeof(a.wind));
+    memcpy(a.sim, sim_desc, sizeof(a.sim));
+    a.drop = w->ellipsoid;
+    memcpy(a.drop_desc, w->ellipsoid_desc, sizeof(a.drop_desc));
+    a.dff = w->dff[les_id];
+    memcpy(a.dff_desc, w->dff_desc, sizeof(a.dff_desc));
+    a.rain_origin = pop->origins[0];
+    a.rain_count = pop->counts[0];
+    /* kernel selection of rs.c:5339-5349 */
+    if (concept & rsc::kConceptDragged) {
+        a.rain_mode = 1;
+    } else if (concept & rsc::kConceptFixedPos) {
+        a.rain_mode = 2;
+    } else {
+        a.rain_mode = 0;
+    }
+    if (a.rain_count && a.rain_mode != 2 && w->ellipsoid == nullptr) {
+        return fail(RSC_ERR_STATE, "ellipsoid RCS table not set");
+    }
+    a.rain_blocks = (unsigned)((a.rain_count + rsc::kAdvanceThreads - 1) / rsc::kAdvanceThreads);
+    unsigned long long deb = 0;
+    s = fill_debris(w, pop, a, &deb);
+    if (s) return s;
+    if ((concept & rsc::kConceptDFF) && deb && a.dff == nullptr) return fail(RSC_ERR_STATE, "debris flux field not set");
+    unsigned blocks = a.rain_blocks + (unsigned)((deb + rsc::kAdvanceThreads - 1) / rsc::kAdvanceThreads);
+    if (blocks == 0) return RSC_OK;
+    rsc::k_advance<<<blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
+    RSC_CUDA(cudaGetLastError());
+    w->launches++;
+    w->sig_aux_stale = true;
+    return RSC_OK;
+}
+
+int rsc_update_debris_rcs(rsc_worker *w, const rsc_population *pop, const float sim_desc[16]) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (pop == nullptr || sim_desc == nullptr) return fail(RSC_ERR_ARG, "population / sim_desc is NULL");
+    AdvanceArgs a;
+    memset(&a, 0, sizeof(a));
+    a.pos = w->pos;
+    a.ori = w->ori;
+    a.rcs = w->rcs;
+    memcpy(a.sim, sim_desc, sizeof(a.sim));
+    unsigned long long deb = 0;
+    s = fill_debris(w, pop, a, &deb);
+    if (s) return s;
+    if (deb == 0) return RSC_OK;
+    unsigned blocks = (unsigned)((deb + rsc::kAdvanceThreads - 1) / rsc::kAdvanceThreads);
+    rsc::k_db_rcs<<<blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
+    RSC_CUDA(cudaGetLastError());
+    w->launches++;
+    return RSC_OK;
+}
+
+int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (sim_desc == nullptr) return fail(RSC_ERR_ARG, "sim_desc is NULL");
+    if (w->range_weight == nullptr || w->angular_weight == nullptr) {
+        return fail(RSC_ERR_STATE, "range / angular weight tables not set");
+    }
+    const int mode = w->precision;
+    int grid = 0, threads = 0;
+    size_t smem = 0;
+    s = pulse_geometry(w, mode, &grid, &threads, &smem);
+    if (s) return s;
+    size_t need = (size_t)grid * w->G * 4 * 8;
+    if (need > w->partials_bytes) return fail(RSC_ERR_STATE, "partials buffer too small");
+    PulseArgs P;
+    fill_pulse_args(w, P, sim_desc);
+    if (mode == RSC_PULSE_COMPENSATED) {
+        P.rk = w->rk_hi;
+    }
+    const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
+    P.materialize = mat ? 1 : 0;
+    if (mode == RSC_PULSE_PLAIN) {
+        rsc::k_pulse<0><<<grid, threads, smem, w->stream>>>(P);
+    } else if (mode == RSC_PULSE_COMPENSATED) {
+        rsc::k_pulse<1><<<grid, threads, smem, w->stream>>>(P);
+    } else {
+        rsc::k_pulse<2><<<grid, threads, smem, w->stream>>>(P);
+    }
+    RSC_CUDA(cudaGetLastError());
+    w->launches++;
+    memcpy(w->last_sim, sim_desc, sizeof(w->last_sim));
+    w->have_pulse_desc = true;
+    w->sig_aux_stale = !mat;
+    return RSC_OK;
+}
+
+int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (pulse4 == nullptr) return fail(RSC_ERR_ARG, "pulse4 is NULL");
+    RSC_CUDA(cudaMemcpyAsync(pulse4, w->pulse, w->G * sizeof(float4), cudaMemcpyDeviceToHost, w->stream));
+    RSC_CUDA(cudaStreamSynchronize(w->stream));
+    for (uint32_t k = 0; k < 4 * w->G; k++) pulse4[k] = pulse4[k] * gain;
+    return RSC_OK;
+}
+
+int rsc_synchronize(rsc_worker *w) {
+    int s = check_worker(w);
+    if (s) return s;
+    RSC_CUDA(cudaStreamSynchronize(w->stream));
+    return RSC_OK;
+}
+
+int rsc_set_pulse_precision(rsc_worker *w, int mode) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (mode != RSC_PULSE_PLAIN && mode != RSC_PULSE_COMPENSATED && mode != RSC_PULSE_F64) {
+        return fail(RSC_ERR_ARG, "precision mode %d", mode);
+    }
+    w->precision = mode;
+    return RSC_OK;
+}
+
+int rsc_set_materialize_sig_aux(rsc_worker *w, int enable) {
+    int s = check_worker(w);
+    if (s) return s;
+    w->materialize = enable ? 1 : 0;
+    return RSC_OK;
+}
+
+int rsc_launch_count(rsc_worker *w, uint64_t *count) {
+    if (w == nullptr || count == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *count = w->launches;
+    return RSC_OK;
+}
+
+int rsc_get_stream(rsc_worker *w, void **stream) {
+    if (w == nullptr || stream == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *stream = (void *)w->stream;
+    return RSC_OK;
+}
+
+int rsc_eval_math(int fn, const float *a, const float *b, float *out, size_t n) {
+    if (a == nullptr || out == nullptr || n == 0) return fail(RSC_ERR_ARG, "eval_math arguments");
+    float *da = nullptr, *db = nullptr, *dout = nullptr;
+    RSC_CUDA(cudaMalloc((void **)&da, n * sizeof(float)));
+    RSC_CUDA(cudaMalloc((void **)&db, n * sizeof(float)));
+    RSC_CUDA(cudaMalloc((void **)&dout, n * sizeof(float)));
+    RSC_CUDA(cudaMemcpy(da, a, n * sizeof(float), cudaMemcpyHostToDevice));
+    RSC_CUDA(cudaMemcpy(db, b ? b : a, n * sizeof(float), cudaMemcpyHostToDevice));
+    rsc::k_eval_math<<<(unsigned)((n + 255) / 256), 256>>>(fn, da, db, dout, n);
+    RSC_CUDA(cudaGetLastError());
+    RSC_CUDA(cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost));
+    cudaFree(da);
+    cudaFree(db);
+    cudaFree(dout);
+    return RSC_OK;
+}
+
+}  // extern "C"

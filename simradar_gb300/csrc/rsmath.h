@@ -1,0 +1,360 @@
+/*
+ * rsmath.h -- portable single-precision elementary functions.
+ *
+ * The OpenCL kernels of SimRadar call log1p, log, acos, atan2, sincos, cos and
+ * pow (rs.cl:151, rs.cl:212-215, rs.cl:268-280, rs.cl:282-359, rs.cl:590-648,
+ * rs.cl:744-907, rs.cl:1050-1110).  OpenCL only bounds their error (several
+ * ulp), so every device and every libm gives slightly different bits.  This
+ * header evaluates each of them with a fixed sequence of IEEE single-precision
+ * operations (add, sub, mul, div, sqrt, floor, rint, copysign: all correctly
+ * rounded), so the CUDA kernels and the CPU oracle produce identical bits on
+ * x86-64 and aarch64 hosts and on sm_103a.  That is what makes the respawn RNG
+ * state, the positions and the scatterer-to-gate indices bit-exact between the
+ * GPU and the oracle even on the stretched LES grid, where log1p feeds the
+ * wind lookup every pulse.
+ *
+ * Methods (all textbook mathematics, coefficients from the Taylor series):
+ *   - sin/cos: Cody-Waite reduction by pi/2 split in three floats, applied
+ *     with fmaf (the first step is exact for |x| < 2^22 * pi/2), then the
+ *     Taylor polynomials of sin (to x^9) and cos (to x^10) on [-pi/4, pi/4].
+ *   - log: x = m 2^e with m in [sqrt(1/2), sqrt(2)), log(m) = 2 atanh(s),
+ *     s = (m-1)/(m+1), series to s^9; e*ln2 added as a 16-bit head + tail.
+ *   - log1p: Goldberg's identity log1p(x) = log(u) * x / (u - 1), u = 1 + x
+ *     (D. Goldberg, "What every computer scientist should know about
+ *     floating-point arithmetic", ACM Computing Surveys 23(1), 1991, thm. 4).
+ *   - asin/acos: Taylor series of asin to s^21 on |s| <= 1/2 and the
+ *     half-angle identity acos(x) = 2 asin(sqrt((1-x)/2)) above.
+ *   - atan/atan2: reduction to [0, 1], then to |u| <= tan(pi/8) by
+ *     atan(t) = pi/4 + atan((t-1)/(t+1)), Taylor series to u^19.
+ *   - exp: k = rint(x/ln2), r = x - k ln2 (two-part), Taylor to r^7, 2^k by
+ *     exponent construction.  pow(b, e) = exp(e log b) with the rounding error
+ *     of the product carried by fmaf.
+ *
+ * Polynomials are evaluated with fmaf (one correctly rounded operation on both
+ * the CPU and the GPU).  The CUDA translation unit that includes this header
+ * is compiled with -fmad=false and the oracle with -ffp-contract=off, so any
+ * "a * b + c" not written as fmaf is two rounded operations on both sides.
+ * Measured accuracy against float64 references is checked by the CPU tests.
+ */
+#ifndef SIMRADAR_GB300_RSMATH_H
+#define SIMRADAR_GB300_RSMATH_H
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define RSM_FN static __host__ __device__ __forceinline__
+#else
+#define RSM_FN static inline
+#endif
+
+/* pi/2 in three floats; pi and pi/2 as head + tail */
+#define RSM_PIO2_1   0x1.921fb6p+0f
+#define RSM_PIO2_2  (-0x1.777a5cp-25f)
+#define RSM_PIO2_3  (-0x1.ee59dap-50f)
+#define RSM_PI_HI    0x1.921fb6p+1f
+#define RSM_PI_LO   (-0x1.777a5cp-24f)
+#define RSM_PIO2_HI  0x1.921fb6p+0f
+#define RSM_PIO2_LO (-0x1.777a5cp-25f)
+#define RSM_PIO4_HI  0x1.921fb6p-1f
+#define RSM_PIO4_LO (-0x1.777a5cp-26f)
+#define RSM_LN2_HI   0x1.62e400p-1f
+#define RSM_LN2_LO   0x1.7f7d1cp-20f
+#define RSM_TWO_OVER_PI 0x1.45f306p-1f
+#define RSM_INV_LN2  0x1.715476p+0f
+#define RSM_SQRT2    0x1.6a09e6p+0f
+#define RSM_TAN_PIO8 0x1.a8279ap-2f
+
+RSM_FN uint32_t rsm_f2u(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, sizeof(u));
+    return u;
+#endif
+}
+
+RSM_FN float rsm_u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, sizeof(f));
+    return f;
+#endif
+}
+
+RSM_FN int rsm_isnan(float x) { return x != x; }
+
+/* 2^k for k in [-149, 127] (exact) */
+RSM_FN float rsm_exp2i(int k) {
+    if (k >= -126) {
+        return rsm_u2f((uint32_t)(k + 127) << 23);
+    }
+    return rsm_u2f(1u << (uint32_t)(k + 149));
+}
+
+/* x - q pi/2 for q = rint(x 2/pi); the first step is exact for |x| < 2^22 pi/2 */
+RSM_FN float rsm_reduce_pio2(float x, float *q_out) {
+    float q = rintf(x * RSM_TWO_OVER_PI);
+    float r = fmaf(-q, RSM_PIO2_1, x);
+    r = fmaf(-q, RSM_PIO2_2, r);
+    r = fmaf(-q, RSM_PIO2_3, r);
+    *q_out = q;
+    return r;
+}
+
+/* sin and cos of (r + q pi/2) for a reduced argument |r| <~ pi/4 and an
+ * integer-valued float q */
+RSM_FN void rsm_sincos_reduced(float r, float q, float *s_out, float *c_out) {
+    float z = r * r;
+    /* sin(r) = r + r z (-1/6 + z (1/120 + z (-1/5040 + z / 362880))) */
+    float ps = 0x1.71de3ap-19f;              /*  1/362880 */
+    ps = fmaf(ps, z, (-0x1.a01a02p-13f));        /* -1/5040   */
+    ps = fmaf(ps, z, 0x1.111112p-7f);            /*  1/120    */
+    ps = fmaf(ps, z, (-0x1.555556p-3f));         /* -1/6      */
+    float sn = fmaf(r * z, ps, r);
+    /* cos(r) = 1 + z (-1/2 + z (1/24 + z (-1/720 + z (1/40320 - z / 3628800)))) */
+    float pc = -0x1.27e4fcp-22f;             /* -1/3628800 */
+    pc = fmaf(pc, z, 0x1.a01a02p-16f);           /*  1/40320   */
+    pc = fmaf(pc, z, (-0x1.6c16c2p-10f));        /* -1/720     */
+    pc = fmaf(pc, z, 0x1.555556p-5f);            /*  1/24      */
+    pc = fmaf(pc, z, (-0.5f));
+    float cs = fmaf(z, pc, 1.0f);
+    /* quadrant from the low two bits of q (q is an integer-valued float) */
+    float q4 = q - 4.0f * floorf(q * 0.25f);
+    int quad = (int)q4;
+    float s, c;
+    switch (quad & 3) {
+        case 0: s = sn; c = cs; break;
+        case 1: s = cs; c = -sn; break;
+        case 2: s = -sn; c = -cs; break;
+        default: s = -cs; c = sn; break;
+    }
+    *s_out = s;
+    *c_out = c;
+}
+
+/* sin and cos of x.  Accurate for |x| < 6.7e6; beyond that the reduction
+ * loses bits (the kernels never pass such phases: k*r at 30 km is 3.8e6). */
+RSM_FN void rsm_sincosf(float x, float *s_out, float *c_out) {
+    if (!(fabsf(x) < INFINITY)) {
+        float n = x - x;
+        *s_out = n;
+        *c_out = n;
+        return;
+    }
+    float q;
+    float r = rsm_reduce_pio2(x, &q);
+    rsm_sincos_reduced(r, q, s_out, c_out);
+}
+
+RSM_FN float rsm_sinf(float x) {
+    float s, c;
+    rsm_sincosf(x, &s, &c);
+    return s;
+}
+
+RSM_FN float rsm_cosf(float x) {
+    float s, c;
+    rsm_sincosf(x, &s, &c);
+    return c;
+}
+
+/* natural logarithm */
+RSM_FN float rsm_logf(float x) {
+    if (rsm_isnan(x) || x < 0.0f) {
+        return (x - x) / (x - x);            /* NaN */
+    }
+    if (x == 0.0f) {
+        return -INFINITY;
+    }
+    if (x == INFINITY) {
+        return x;
+    }
+    int e = 0;
+    if (x < 0x1p-126f) {                      /* subnormal: scale up (exact) */
+        x = x * 0x1p23f;
+        e = -23;
+    }
+    uint32_t u = rsm_f2u(x);
+    e += (int)((u >> 23) & 0xff) - 127;
+    float m = rsm_u2f((u & 0x007fffffu) | 0x3f800000u);   /* [1, 2) */
+    if (m > RSM_SQRT2) {
+        m = m * 0.5f;                         /* exact */
+        e += 1;
+    }
+    float f = m - 1.0f;                       /* exact (Sterbenz) */
+    float s = f / (2.0f + f);
+    float z = s * s;
+    /* 2 atanh(s) = 2 s + s z (2/3 + z (2/5 + z (2/7 + z 2/9))) */
+    float p = 0x1.c71c72p-3f;                 /* 2/9 */
+    p = fmaf(p, z, 0x1.24924ap-2f);               /* 2/7 */
+    p = fmaf(p, z, 0x1.99999ap-2f);               /* 2/5 */
+    p = fmaf(p, z, 0x1.555556p-1f);               /* 2/3 */
+    float lm = fmaf(s * z, p, 2.0f * s);
+    float fe = (float)e;
+    return fe * RSM_LN2_HI + fmaf(fe, RSM_LN2_LO, lm);
+}
+
+/* log(1 + x) */
+RSM_FN float rsm_log1pf(float x) {
+    if (rsm_isnan(x)) {
+        return x;
+    }
+    float u = 1.0f + x;
+    if (u == 1.0f) {
+        return x;
+    }
+    if (u == INFINITY) {
+        return rsm_logf(x);
+    }
+    return rsm_logf(u) * (x / (u - 1.0f));
+}
+
+/* asin on |s| <= 1/2 : s + s z P(z), z = s^2 (Taylor series to s^21) */
+RSM_FN float rsm_asin_core(float s, float z) {
+    float p = 0x1.12ef3cp-7f;                 /* c10 =  46189/5505024 */
+    p = fmaf(p, z, 0x1.3fde50p-7f);               /* c9  =  12155/1245184 */
+    p = fmaf(p, z, 0x1.7a8788p-7f);               /* c8  =   6435/557056  */
+    p = fmaf(p, z, 0x1.c9999ap-7f);               /* c7  =    143/10240   */
+    p = fmaf(p, z, 0x1.1c4ec4p-6f);               /* c6  =    231/13312   */
+    p = fmaf(p, z, 0x1.6e8ba2p-6f);               /* c5  =     63/2816    */
+    p = fmaf(p, z, 0x1.f1c71cp-6f);               /* c4  =     35/1152    */
+    p = fmaf(p, z, 0x1.6db6dcp-5f);               /* c3  =      5/112     */
+    p = fmaf(p, z, 0x1.333334p-4f);               /* c2  =      3/40      */
+    p = fmaf(p, z, 0x1.555556p-3f);               /* c1  =      1/6       */
+    return fmaf(s * z, p, s);
+}
+
+RSM_FN float rsm_acosf(float x) {
+    float ax = fabsf(x);
+    if (rsm_isnan(x) || ax > 1.0f) {
+        return (x - x) / (x - x);
+    }
+    if (ax <= 0.5f) {
+        float a = rsm_asin_core(x, x * x);
+        return RSM_PIO2_HI - (a - RSM_PIO2_LO);
+    }
+    float z = (1.0f - ax) * 0.5f;             /* exact */
+    float s = sqrtf(z);
+    float a = 2.0f * rsm_asin_core(s, z);
+    if (x > 0.0f) {
+        return a;
+    }
+    return RSM_PI_HI - (a - RSM_PI_LO);
+}
+
+/* atan on |u| <= tan(pi/8) : u + u z Q(z), Taylor series to u^19 */
+RSM_FN float rsm_atan_core(float u) {
+    float z = u * u;
+    float q = -0x1.af286cp-5f;                /* -1/19 */
+    q = fmaf(q, z, 0x1.e1e1e2p-5f);               /*  1/17 */
+    q = fmaf(q, z, (-0x1.111112p-4f));            /* -1/15 */
+    q = fmaf(q, z, 0x1.3b13b2p-4f);               /*  1/13 */
+    q = fmaf(q, z, (-0x1.745d18p-4f));            /* -1/11 */
+    q = fmaf(q, z, 0x1.c71c72p-4f);               /*  1/9  */
+    q = fmaf(q, z, (-0x1.24924ap-3f));            /* -1/7  */
+    q = fmaf(q, z, 0x1.99999ap-3f);               /*  1/5  */
+    q = fmaf(q, z, (-0x1.555556p-2f));            /* -1/3  */
+    return fmaf(u * z, q, u);
+}
+
+/* atan of t in [0, 1] */
+RSM_FN float rsm_atan01(float t) {
+    if (t > RSM_TAN_PIO8) {
+        float u = (t - 1.0f) / (t + 1.0f);
+        return RSM_PIO4_HI + (rsm_atan_core(u) + RSM_PIO4_LO);
+    }
+    return rsm_atan_core(t);
+}
+
+RSM_FN float rsm_atan2f(float y, float x) {
+    if (rsm_isnan(x) || rsm_isnan(y)) {
+        return x + y;
+    }
+    float ax = fabsf(x);
+    float ay = fabsf(y);
+    float a;
+    if (ay == 0.0f) {
+        /* atan2(+-0, x) = +-0 for x > 0 or x = +0, +-pi for x < 0 or x = -0 */
+        a = (x < 0.0f || (x == 0.0f && (rsm_f2u(x) >> 31))) ? RSM_PI_HI : 0.0f;
+        return copysignf(a, y);
+    }
+    if (ax == INFINITY || ay == INFINITY) {
+        if (ax == INFINITY && ay == INFINITY) {
+            a = x > 0.0f ? RSM_PIO4_HI : 3.0f * RSM_PIO4_HI;
+        } else if (ax == INFINITY) {
+            a = x > 0.0f ? 0.0f : RSM_PI_HI;
+        } else {
+            a = RSM_PIO2_HI;
+        }
+        return copysignf(a, y);
+    }
+    if (ay > ax) {
+        a = rsm_atan01(ax / ay);
+        a = RSM_PIO2_HI - (a - RSM_PIO2_LO);
+    } else {
+        a = rsm_atan01(ay / ax);
+    }
+    if (x < 0.0f) {
+        a = RSM_PI_HI - (a - RSM_PI_LO);
+    }
+    return copysignf(a, y);
+}
+
+/* e^x */
+RSM_FN float rsm_expf(float x) {
+    if (rsm_isnan(x)) {
+        return x;
+    }
+    if (x > 88.7228394f) {
+        return INFINITY;
+    }
+    if (x < -103.972076f) {
+        return 0.0f;
+    }
+    float k = rintf(x * RSM_INV_LN2);
+    float r = fmaf(-k, RSM_LN2_LO, x - k * RSM_LN2_HI);
+    /* e^r, |r| <= ln2/2, Taylor series to r^7 */
+    float p = 0x1.a01a02p-13f;                /* 1/5040 */
+    p = fmaf(p, r, 0x1.6c16c2p-10f);              /* 1/720  */
+    p = fmaf(p, r, 0x1.111112p-7f);               /* 1/120  */
+    p = fmaf(p, r, 0x1.555556p-5f);               /* 1/24   */
+    p = fmaf(p, r, 0x1.555556p-3f);               /* 1/6    */
+    p = fmaf(p, r, 0.5f);
+    float er = 1.0f + fmaf(r * r, p, r);
+    int ki = (int)k;
+    if (ki > 127) {
+        return (er * 2.0f) * rsm_exp2i(ki - 1);
+    }
+    if (ki < -125) {
+        return (er * rsm_exp2i(ki + 64)) * 0x1p-64f;
+    }
+    return er * rsm_exp2i(ki);
+}
+
+/* b^e for b >= 0 (the kernels raise 10 and the stretch ratios) */
+RSM_FN float rsm_powf(float b, float e) {
+    if (e == 0.0f || b == 1.0f) {
+        return 1.0f;
+    }
+    if (rsm_isnan(b) || rsm_isnan(e)) {
+        return b + e;
+    }
+    if (b < 0.0f) {
+        return (b - b) / (b - b);
+    }
+    if (b == 0.0f) {
+        return e > 0.0f ? 0.0f : INFINITY;
+    }
+    float l = rsm_logf(b);
+    float p = e * l;
+    float perr = fmaf(e, l, -p);             /* rounding error of e * l */
+    float r = rsm_expf(p);
+    return fmaf(r, perr, r);
+}
+
+#endif /* SIMRADAR_GB300_RSMATH_H */

@@ -1,0 +1,304 @@
+"""ctypes binding of the backend C ABI (include/rsc.h).
+
+The shared library is the product; this module only marshals numpy arrays
+(float32 / uint32, C-contiguous) into the plain pointers the ABI takes.  There
+is no other implementation behind it: if the library is missing, importing
+the backend raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+RSC_OK = 0
+RSC_MAX_TYPES = 8
+RSC_MAX_GATES = 512
+PULSE_PLAIN = 0
+PULSE_COMPENSATED = 1
+PULSE_F64 = 2
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+
+class BackendError(RuntimeError):
+    """A backend call returned a negative status."""
+
+    def __init__(self, status, message):
+        super().__init__("rsc status %d: %s" % (status, message))
+        self.status = status
+
+
+class Population(ctypes.Structure):
+    """rsc_population: per-type (origin, count) and the ADM / RCS table each
+    debris type uses (RSWorker.origins / .counts, rs.h:160-161)."""
+
+    _fields_ = [
+        ("origins", ctypes.c_uint64 * RSC_MAX_TYPES),
+        ("counts", ctypes.c_uint64 * RSC_MAX_TYPES),
+        ("adm_index", ctypes.c_int32 * RSC_MAX_TYPES),
+        ("rcs_index", ctypes.c_int32 * RSC_MAX_TYPES),
+    ]
+
+    @classmethod
+    def make(cls, counts, origins=None, adm_index=None, rcs_index=None):
+        p = cls()
+        counts = list(counts) + [0] * (RSC_MAX_TYPES - len(counts))
+        if origins is None:
+            origins, acc = [], 0
+            for c in counts:
+                origins.append(acc)
+                acc += c
+        origins = list(origins) + [0] * (RSC_MAX_TYPES - len(origins))
+        for k in range(RSC_MAX_TYPES):
+            p.origins[k] = int(origins[k])
+            p.counts[k] = int(counts[k])
+            p.adm_index[k] = int(adm_index[k]) if adm_index is not None else max(k - 1, 0)
+            p.rcs_index[k] = int(rcs_index[k]) if rcs_index is not None else max(k - 1, 0)
+        return p
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load_library():
+    """Load libsimradar_gb300.so (built by simradar_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise ImportError("simradar_gb300 backend library not built: %s (run simradar_gb300.build.build())" % path)
+    lib = ctypes.CDLL(path)
+    P, I, S, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_float
+    sig = {
+        "rsc_last_error": ([], ctypes.c_char_p),
+        "rsc_device_count": ([ctypes.POINTER(I)], I),
+        "rsc_worker_create": ([I, ctypes.POINTER(P)], I),
+        "rsc_worker_free": ([P], I),
+        "rsc_worker_malloc": ([P, S, F, F, U32], I),
+        "rsc_set_range_weight": ([P, _f32p, U32, _f32p], I),
+        "rsc_set_angular_weight": ([P, _f32p, U32, _f32p], I),
+        "rsc_set_rcs_ellipsoid": ([P, _f32p, U32, _f32p], I),
+        "rsc_set_les": ([P, I, _f32p, _f32p, U32, U32, U32, _f32p], I),
+        "rsc_set_les_async": ([P, I, _f32p, _f32p, U32, U32, U32, _f32p], I),
+        "rsc_set_adm": ([P, I, _f32p, _f32p, U32, U32, _f32p], I),
+        "rsc_set_rcs": ([P, I, _f32p, _f32p, U32, U32, _f32p], I),
+        "rsc_set_dff": ([P, I, _f32p, U32, _f32p], I),
+        "rsc_upload": ([P, S, S, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _u32p], I),
+        "rsc_download": ([P, S, S, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _u32p], I),
+        "rsc_advance_time": ([P, ctypes.POINTER(Population), I, _f32p], I),
+        "rsc_update_debris_rcs": ([P, ctypes.POINTER(Population), _f32p], I),
+        "rsc_make_pulse": ([P, _f32p], I),
+        "rsc_download_pulse": ([P, _f32p, F], I),
+        "rsc_synchronize": ([P], I),
+        "rsc_set_pulse_precision": ([P, I], I),
+        "rsc_set_materialize_sig_aux": ([P, I], I),
+        "rsc_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
+        "rsc_get_stream": ([P, ctypes.POINTER(P)], I),
+        "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
+    }
+    for name, (argtypes, restype) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = restype
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != RSC_OK:
+        raise BackendError(status, load_library().rsc_last_error().decode(errors="replace"))
+
+
+def _fp(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"], "expected C-contiguous float32"
+    return a.ctypes.data_as(_f32p)
+
+
+def _up(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint32 and a.flags["C_CONTIGUOUS"], "expected C-contiguous uint32"
+    return a.ctypes.data_as(_u32p)
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def device_count():
+    n = ctypes.c_int(0)
+    _check(load_library().rsc_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def eval_math(fn, a, b=None):
+    a = f32(a)
+    b = f32(b) if b is not None else None
+    out = np.empty_like(a)
+    _check(load_library().rsc_eval_math(int(fn), _fp(a), _fp(b), _fp(out), a.size))
+    return out
+
+
+FIELDS = ("pos", "vel", "ori", "tum", "aux", "rcs", "sig", "rnd")
+
+
+class Worker:
+    """One GPU worker (RSWorker, rs.h:150-266) behind the C ABI."""
+
+    def __init__(self, device=0):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.rsc_worker_create(int(device), ctypes.byref(h)))
+        self._h = h
+        self.num_scats = 0
+        self.range_count = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rsc_worker_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # --- allocation and tables -------------------------------------------
+    def malloc(self, num_scats, range_start, range_delta, range_count):
+        _check(self._lib.rsc_worker_malloc(self._h, int(num_scats), float(range_start), float(range_delta),
+                                           int(range_count)))
+        self.num_scats = int(num_scats)
+        self.range_count = int(range_count)
+
+    def set_range_weight(self, table, desc):
+        t, d = f32(table), f32(desc)
+        _check(self._lib.rsc_set_range_weight(self._h, _fp(t), t.size, _fp(d)))
+
+    def set_angular_weight(self, table, desc):
+        t, d = f32(table), f32(desc)
+        _check(self._lib.rsc_set_angular_weight(self._h, _fp(t), t.size, _fp(d)))
+
+    def set_rcs_ellipsoid(self, table4, desc):
+        t, d = f32(table4), f32(desc)
+        _check(self._lib.rsc_set_rcs_ellipsoid(self._h, _fp(t), t.size // 4, _fp(d)))
+
+    def set_les(self, slot, uvwt, cpxx, desc, asynchronous=False):
+        """uvwt, cpxx: (nz, ny, nx, 4) float32."""
+        u = f32(uvwt)
+        c = f32(cpxx) if cpxx is not None else None
+        d = f32(desc)
+        nz, ny, nx = u.shape[:3]
+        fn = self._lib.rsc_set_les_async if asynchronous else self._lib.rsc_set_les
+        _check(fn(self._h, int(slot), _fp(u), _fp(c), nx, ny, nz, _fp(d)))
+        if asynchronous:
+            self._keep = (u, c)
+
+    def set_adm(self, index, cd, cm, desc):
+        """cd, cm: (ny, nx, 4) float32 (x = beta, y = alpha)."""
+        a, b, d = f32(cd), f32(cm), f32(desc)
+        ny, nx = a.shape[:2]
+        _check(self._lib.rsc_set_adm(self._h, int(index), _fp(a), _fp(b), nx, ny, _fp(d)))
+
+    def set_rcs(self, index, real, imag, desc):
+        """real, imag: (ny, nx, 4) float32 (x = alpha, y = beta)."""
+        a, b, d = f32(real), f32(imag), f32(desc)
+        ny, nx = a.shape[:2]
+        _check(self._lib.rsc_set_rcs(self._h, int(index), _fp(a), _fp(b), nx, ny, _fp(d)))
+
+    def set_dff(self, slot, icdf, desc):
+        t, d = f32(icdf), f32(desc)
+        _check(self._lib.rsc_set_dff(self._h, int(slot), _fp(t), t.size, _fp(d)))
+
+    # --- state -----------------------------------------------------------
+    def upload(self, offset=0, **arrays):
+        count = None
+        ptrs = []
+        keep = []
+        for f in FIELDS:
+            a = arrays.get(f)
+            if a is None:
+                ptrs.append(None)
+                continue
+            a = np.ascontiguousarray(a, dtype=np.uint32 if f == "rnd" else np.float32)
+            keep.append(a)
+            n = a.size // 4
+            if count is None:
+                count = n
+            elif count != n:
+                raise ValueError("arrays of different lengths")
+            ptrs.append(_up(a) if f == "rnd" else _fp(a))
+        if count is None:
+            return
+        _check(self._lib.rsc_upload(self._h, int(offset), int(count), *ptrs))
+
+    def download(self, fields=FIELDS, offset=0, count=None):
+        if count is None:
+            count = self.num_scats - offset
+        out = {}
+        ptrs = []
+        for f in FIELDS:
+            if f in fields:
+                a = np.empty((count, 4), dtype=np.uint32 if f == "rnd" else np.float32)
+                out[f] = a
+                ptrs.append(_up(a) if f == "rnd" else _fp(a))
+            else:
+                ptrs.append(None)
+        _check(self._lib.rsc_download(self._h, int(offset), int(count), *ptrs))
+        return out
+
+    # --- hot path --------------------------------------------------------
+    def advance_time(self, pop, les_id, sim_desc):
+        d = f32(sim_desc)
+        _check(self._lib.rsc_advance_time(self._h, ctypes.byref(pop), int(les_id), _fp(d)))
+
+    def update_debris_rcs(self, pop, sim_desc):
+        d = f32(sim_desc)
+        _check(self._lib.rsc_update_debris_rcs(self._h, ctypes.byref(pop), _fp(d)))
+
+    def make_pulse(self, sim_desc):
+        d = f32(sim_desc)
+        _check(self._lib.rsc_make_pulse(self._h, _fp(d)))
+
+    def download_pulse(self, gain=1.0, out=None):
+        if out is None:
+            out = np.empty((self.range_count, 4), dtype=np.float32)
+        _check(self._lib.rsc_download_pulse(self._h, _fp(out), float(gain)))
+        return out
+
+    def synchronize(self):
+        _check(self._lib.rsc_synchronize(self._h))
+
+    def set_precision(self, mode):
+        _check(self._lib.rsc_set_pulse_precision(self._h, int(mode)))
+
+    def set_materialize(self, enable):
+        _check(self._lib.rsc_set_materialize_sig_aux(self._h, 1 if enable else 0))
+
+    @property
+    def launch_count(self):
+        n = ctypes.c_uint64(0)
+        _check(self._lib.rsc_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(self._lib.rsc_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
