@@ -21,7 +21,9 @@
  *     s = (m-1)/(m+1), series to s^9; e*ln2 added as a 16-bit head + tail.
  *   - log1p: Goldberg's identity log1p(x) = log(u) * x / (u - 1), u = 1 + x
  *     (D. Goldberg, "What every computer scientist should know about
- *     floating-point arithmetic", ACM Computing Surveys 23(1), 1991, thm. 4).
+ *     floating-point arithmetic", ACM Computing Surveys 23(1), 1991, thm. 4)
+ *     outside sqrt(1/2) - 1 < x < sqrt(2) - 1, the atanh series on
+ *     s = x / (2 + x) inside.
  *   - asin/acos: Taylor series of asin to s^21 on |s| <= 1/2 and the
  *     half-angle identity acos(x) = 2 asin(sqrt((1-x)/2)) above.
  *   - atan/atan2: reduction to [0, 1], then to |u| <= tan(pi/8) by
@@ -163,6 +165,17 @@ RSM_FN float rsm_cosf(float x) {
     return c;
 }
 
+/* log((1 + s) / (1 - s)) = 2 atanh(s) = 2 s + s z (2/3 + z (2/5 + z (2/7 + z 2/9))),
+ * z = s^2, for |s| <= 3 - 2 sqrt(2) */
+RSM_FN float rsm_log_core(float s) {
+    float z = s * s;
+    float p = 0x1.c71c72p-3f;                 /* 2/9 */
+    p = fmaf(p, z, 0x1.24924ap-2f);           /* 2/7 */
+    p = fmaf(p, z, 0x1.99999ap-2f);           /* 2/5 */
+    p = fmaf(p, z, 0x1.555556p-1f);           /* 2/3 */
+    return fmaf(s * z, p, 2.0f * s);
+}
+
 /* natural logarithm */
 RSM_FN float rsm_logf(float x) {
     if (rsm_isnan(x) || x < 0.0f) {
@@ -187,14 +200,7 @@ RSM_FN float rsm_logf(float x) {
         e += 1;
     }
     float f = m - 1.0f;                       /* exact (Sterbenz) */
-    float s = f / (2.0f + f);
-    float z = s * s;
-    /* 2 atanh(s) = 2 s + s z (2/3 + z (2/5 + z (2/7 + z 2/9))) */
-    float p = 0x1.c71c72p-3f;                 /* 2/9 */
-    p = fmaf(p, z, 0x1.24924ap-2f);               /* 2/7 */
-    p = fmaf(p, z, 0x1.99999ap-2f);               /* 2/5 */
-    p = fmaf(p, z, 0x1.555556p-1f);               /* 2/3 */
-    float lm = fmaf(s * z, p, 2.0f * s);
+    float lm = rsm_log_core(f / (2.0f + f));
     float fe = (float)e;
     return fe * RSM_LN2_HI + fmaf(fe, RSM_LN2_LO, lm);
 }
@@ -203,6 +209,11 @@ RSM_FN float rsm_logf(float x) {
 RSM_FN float rsm_log1pf(float x) {
     if (rsm_isnan(x)) {
         return x;
+    }
+    if (x > -0x1.2bec34p-2f && x < 0x1.a8279ap-2f) {
+        /* 1 + x in [sqrt(1/2), sqrt(2)): the series on s = x / (2 + x)
+         * directly, without rounding 1 + x */
+        return rsm_log_core(x / (2.0f + x));
     }
     float u = 1.0f + x;
     if (u == 1.0f) {

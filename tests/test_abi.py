@@ -1,0 +1,57 @@
+"""The C ABI library builds, loads without a GPU and exports every entry
+point include/rsc.h declares; calls report status codes instead of exiting."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "rsc.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rsc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    syms = declared_symbols()
+    for s in ("rsc_worker_create", "rsc_worker_malloc", "rsc_set_les", "rsc_set_adm", "rsc_set_rcs",
+              "rsc_upload", "rsc_download", "rsc_advance_time", "rsc_make_pulse", "rsc_download_pulse"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(backend):
+    lib = backend.load_library()
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, "not exported: %s" % missing
+
+
+def test_null_arguments_return_status(backend):
+    lib = backend.load_library()
+    assert lib.rsc_worker_create(0, None) == -1
+    assert lib.rsc_device_count(None) == -1
+    assert lib.rsc_make_pulse(None, None) == -1
+    assert lib.rsc_advance_time(None, None, 0, None) == -1
+    assert b"NULL" in lib.rsc_last_error()
+    assert lib.rsc_worker_free(None) == 0
+
+
+def test_product_does_not_load_the_oracle():
+    """The package never imports the oracle (test infrastructure)."""
+    pkg = os.path.join(ROOT, "simradar_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            if fn.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                with open(os.path.join(dirpath, fn)) as f:
+                    src = f.read()
+                assert "oracle" not in re.sub(r"(#|//|/\*|\*).*", "", src), fn
+
+
+@pytest.mark.parametrize("sym", ["rsc_eval_math", "rsc_set_pulse_precision"])
+def test_cdll_signature(backend, sym):
+    lib = backend.load_library()
+    fn = getattr(lib, sym)
+    assert fn.restype is ctypes.c_int

@@ -1,0 +1,68 @@
+"""Accuracy of the shared single-precision elementary functions (rsmath.h)
+against float64 references, evaluated through the oracle build."""
+import numpy as np
+import pytest
+
+
+def ulp32(x):
+    x = np.abs(np.asarray(x, dtype=np.float32))
+    return np.spacing(x).astype(np.float64)
+
+
+CASES = [
+    # fn, name, generator, reference, max ulp
+    (0, "sin", lambda r: r.uniform(-20, 20, 200000), lambda a, b: np.sin(a), 2.0),
+    (1, "cos", lambda r: r.uniform(-20, 20, 200000), lambda a, b: np.cos(a), 2.0),
+    (0, "sin large", lambda r: r.uniform(1e5, 4e6, 200000), lambda a, b: np.sin(a), 4.0),
+    (1, "cos large", lambda r: r.uniform(1e5, 4e6, 200000), lambda a, b: np.cos(a), 4.0),
+    (2, "log", lambda r: np.exp(r.uniform(-30, 30, 200000)), lambda a, b: np.log(a), 2.0),
+    (3, "log1p", lambda r: r.uniform(-0.9, 20, 200000), lambda a, b: np.log1p(a), 3.0),
+    (4, "acos", lambda r: r.uniform(-1, 1, 200000), lambda a, b: np.arccos(a), 2.0),
+    (6, "exp", lambda r: r.uniform(-80, 80, 200000), lambda a, b: np.exp(a), 2.0),
+]
+
+
+@pytest.mark.parametrize("fn,name,gen,ref,bound", CASES, ids=[c[1] for c in CASES])
+def test_unary_accuracy(oracle_lib, fn, name, gen, ref, bound):
+    rng = np.random.default_rng(fn + 11)
+    a = gen(rng).astype(np.float32)
+    got = oracle_lib.eval_math(fn, a).astype(np.float64)
+    want = ref(a.astype(np.float64), None)
+    err = np.abs(got - want) / ulp32(want)
+    assert err.max() <= bound, "%s: max error %.3f ulp" % (name, err.max())
+
+
+def test_atan2_accuracy(oracle_lib):
+    rng = np.random.default_rng(5)
+    y = rng.uniform(-10, 10, 200000).astype(np.float32)
+    x = rng.uniform(-10, 10, 200000).astype(np.float32)
+    got = oracle_lib.eval_math(5, y, x).astype(np.float64)
+    want = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    assert (np.abs(got - want) / ulp32(want)).max() <= 3.0
+
+
+def test_atan2_special_values(oracle_lib):
+    y = np.array([0.0, -0.0, 0.0, -0.0, 1.0, -1.0, 0.0, 5.0], dtype=np.float32)
+    x = np.array([1.0, 1.0, -1.0, -1.0, 0.0, 0.0, 0.0, np.inf], dtype=np.float32)
+    got = oracle_lib.eval_math(5, y, x)
+    want = np.arctan2(y, x)
+    assert np.allclose(got, want, rtol=1e-6, atol=0) and np.array_equal(np.signbit(got), np.signbit(want))
+
+
+def test_pow_accuracy(oracle_lib):
+    rng = np.random.default_rng(9)
+    e = rng.uniform(-20, 5, 200000).astype(np.float32)
+    got = oracle_lib.eval_math(7, np.full_like(e, 10.0), e).astype(np.float64)
+    want = 10.0 ** e.astype(np.float64)
+    # OpenCL allows pow 16 ulp
+    assert (np.abs(got - want) / ulp32(want)).max() <= 16.0
+
+
+def test_special_inputs(oracle_lib):
+    nan = np.float32(np.nan)
+    assert np.isnan(oracle_lib.eval_math(2, np.array([-1.0, nan], np.float32))).all()
+    assert oracle_lib.eval_math(2, np.array([0.0], np.float32))[0] == -np.inf
+    assert np.isnan(oracle_lib.eval_math(4, np.array([1.5, -1.01], np.float32))).all()
+    assert oracle_lib.eval_math(3, np.array([1e-30], np.float32))[0] == np.float32(1e-30)
+    assert np.isnan(oracle_lib.eval_math(0, np.array([np.inf], np.float32)))[0]
+    assert oracle_lib.eval_math(6, np.array([-200.0, 200.0], np.float32)).tolist() == [0.0, np.inf]
