@@ -51,6 +51,8 @@ def lib():
                                     _f, U32, U32, U32, I_]
         L.or_make_pulse.restype = I_
         L.or_make_pulse_f64.argtypes = [_d, _d, _f, _f, S_, _f, _f, _f, _f, ctypes.c_double, ctypes.c_double, U32, _f]
+        L.or_make_pulse_direct.argtypes = [_d, _d, _f, _f, S_, _f, _f, _f, _f, ctypes.c_float, ctypes.c_float, U32,
+                                           _f]
         L.or_eval_math.argtypes = [I_, _f, _f, _f, S_]
         L.or_num_threads.restype = I_
         _lib = L
@@ -165,6 +167,29 @@ def make_pulse(st, S, sim_desc, group_size_multiple=64, max_work_group_size=1024
     if rc != 0:
         raise RuntimeError("or_make_pulse failed: %d" % rc)
     return pulse
+
+
+def make_pulse_direct(st, S, sim_desc, return_abs=False):
+    """The reference's FP32 contributions summed exactly (double), every gate."""
+    L = lib()
+    s = st.s
+    N = s["pos"].shape[0]
+    out = np.zeros((S.range_count, 4), dtype=np.float64)
+    ab = np.zeros((S.range_count, 4), dtype=np.float64)
+    sd = np.ascontiguousarray(sim_desc, dtype=np.float32)
+    L.or_make_pulse_direct(out.ctypes.data_as(_d), ab.ctypes.data_as(_d), fp(s["pos"]), fp(s["rcs"]), N, fp(S.ang_w),
+                           fp(S.ang_desc), fp(S.range_w), fp(S.range_desc), float(S.range_start),
+                           float(S.range_delta), S.range_count, fp(sd))
+    return (out, ab) if return_abs else out
+
+
+def reference_plan_valid(n, group_size_multiple=64):
+    """make_pulse_pass_1's tree needs a power-of-two work-group size
+    (count / 2 when count < 2 * 64) and RS_make_pulse_params needs count >= 2."""
+    if n < 2:
+        return False
+    wi = group_size_multiple if n > 2 * group_size_multiple else n // 2
+    return wi & (wi - 1) == 0
 
 
 def make_pulse_f64(st, S, sim_desc, return_abs=False):

@@ -565,6 +565,9 @@ int or_make_pulse_params(or_pulse_params *P, uint32_t count, uint32_t group_size
         P->user_max_groups = 1024;
     }
     uint32_t work_items = count > P->user_max_work_items * 2 ? P->user_max_work_items : count / 2;
+    if (work_items == 0) {
+        return -3;   /* count < 2: the reference divides by zero on the next line (rs.c:1308-1311) */
+    }
     uint32_t group_count = count <= work_items * 2 ? 1 : (count + work_items * 2 - 1) / (work_items * 2);
     if (group_count > P->user_max_groups) {
         group_count = P->user_max_groups;
@@ -636,7 +639,11 @@ void or_make_pulse_pass_1(of4 *out, const of4 *sig, const of4 *aux, size_t n_all
 #pragma omp parallel for schedule(dynamic, 1)
     for (long long gg = 0; gg < (long long)group_count; gg++) {
         uint32_t group_id = (uint32_t)gg;
-        of4 *shared = (of4 *)calloc((size_t)G * local_size, sizeof(of4));
+        /* local_size extra zero entries: the tree below assumes a power-of-two
+         * local size; with any other size (counts < 128, work_items = count / 2)
+         * it adds entries of the next gate's column, and for the last gate it
+         * reads past the G x local_size array of the reference */
+        of4 *shared = (of4 *)calloc((size_t)G * local_size + local_size, sizeof(of4));
         for (uint32_t lid = 0; lid < local_size; lid++) {
             uint32_t i = group_id * group_stride + lid;
             while (i < n) {
@@ -805,6 +812,56 @@ int or_make_pulse(of4 *pulse, of4 *sig, of4 *aux, const of4 *pos, const of4 *rcs
     free(work);
     free(out);
     return 0;
+}
+
+/* ---- the FP32 per-scatterer, per-gate contributions of scat_sig_aux +
+ * pass 1 (rs.cl:1050-1217: w * (sig * angular weight), the gate origin
+ * advanced by FP32 additions), summed exactly in double ---- */
+void or_make_pulse_direct(double *pulse4, double *abs4, const of4 *pos, const of4 *rcs, size_t n, const float *aw,
+                          const float *awd, const float *rw, const float *rwd, float range_start, float range_delta,
+                          uint32_t G, const float *sd) {
+    memset(pulse4, 0, sizeof(double) * 4 * G);
+    if (abs4) memset(abs4, 0, sizeof(double) * 4 * G);
+    const float xs = rwd[0], x0_0 = rwd[1] + 0.0f, x0_1 = rwd[1] + 1.0f, xm = rwd[2];
+    int nt = or_num_threads();
+    double *acc = (double *)calloc((size_t)nt * 8 * G, sizeof(double));
+#pragma omp parallel
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        double *my = acc + (size_t)tid * 8 * G;
+#pragma omp for schedule(static)
+        for (long long ii = 0; ii < (long long)n; ii++) {
+            of4 sig, aux = f4(0.0f, 0.0f, 0.0f, 0.0f);
+            sig_aux_one(&sig, &aux, pos[ii], rcs[ii], aw, awd, sd);
+            float s[4] = {sig.x * aux.w, sig.y * aux.w, sig.z * aux.w, sig.w * aux.w};
+            float r = range_start;
+            for (uint32_t k = 0; k < G; k++) {
+                float d = aux.x - r;
+                float f0, f1;
+                float dec0 = cl_fract(cl_clamp(fmaf(d, xs, x0_0), 0.0f, xm), &f0);
+                (void)cl_fract(cl_clamp(fmaf(d, xs, x0_1), 0.0f, xm), &f1);
+                float w = cl_mix(rw[cl_f2u_rtz(f0)], rw[cl_f2u_rtz(f1)], dec0);
+                for (int l = 0; l < 4; l++) {
+                    float c = w * s[l];
+                    my[k * 8 + l] += (double)c;
+                    my[k * 8 + 4 + l] += fabs((double)c);
+                }
+                r = r + range_delta;
+            }
+        }
+    }
+    for (int t = 0; t < nt; t++) {
+        for (uint32_t k = 0; k < G; k++) {
+            for (int l = 0; l < 4; l++) {
+                pulse4[k * 4 + l] += acc[((size_t)t * G + k) * 8 + l];
+                if (abs4) abs4[k * 4 + l] += acc[((size_t)t * G + k) * 8 + 4 + l];
+            }
+        }
+    }
+    free(acc);
 }
 
 /* ---- FP64 reference pulse ---- */

@@ -105,6 +105,14 @@ int or_make_pulse(of4 *pulse, of4 *sig, of4 *aux, const of4 *pos, const of4 *rcs
                   const float *sim_desc, uint32_t group_size_multiple, uint32_t max_work_group_size,
                   uint32_t local_mem_size, int name_swap);
 
+/* The FP32 per-scatterer, per-gate contributions exactly as scat_sig_aux and
+ * pass 1 form them (the values the reference adds), summed in double over
+ * every gate: the pulse with the summation-order error removed. */
+void or_make_pulse_direct(double *pulse4, double *abs_sum4, const of4 *pos, const of4 *rcs, size_t num_scats,
+                          const float *angular_weight, const float *angular_weight_desc,
+                          const float *range_weight, const float *range_weight_desc,
+                          float range_start, float range_delta, uint32_t range_count, const float *sim_desc);
+
 /* FP64 pulse of the same FP32 state: the reference of the error metric.
  * Ranges, angles, phases, weights and sums are all evaluated in double; the
  * gate origins are range_start + k * range_delta in double.  Also returns
