@@ -171,6 +171,43 @@ int rsc_launch_count(rsc_worker *w, uint64_t *count);
  * time with events on it). */
 int rsc_get_stream(rsc_worker *w, void **stream);
 
+/* Limits of rsc_make_pulse_noalloc (its scratch is a fixed device array of
+ * about 1.3 MB per GPU that loads this library). */
+#define RSC_NOALLOC_MAX_GATES 128
+#define RSC_NOALLOC_MAX_BLOCKS 640
+#define RSC_NOALLOC_MAX_RANGE_TABLE 64
+#define RSC_NOALLOC_MAX_ANGULAR_TABLE 1024
+
+/* Form a pulse without allocating any device memory.  This entry point has no
+ * counterpart in the reference: it is for callers that cannot call cudaMalloc
+ * -- a real-time pulse loop that must not allocate, an application whose
+ * device memory is owned by another allocator or already fully reserved, or
+ * code whose allocation calls are forbidden while it records work -- and that
+ * already hold the scatterer arrays in their own device buffers.
+ *
+ * Inputs: pos4 and rcs4 are device arrays of num_scats float4; pulse4 is a
+ * device array of range_count float4 that receives the per-gate (Ih, Qh, Iv,
+ * Qv) sums (no gain applied).  The weight tables, their descriptors and
+ * sim_desc are host arrays, copied before the launch.  The pulse is the one
+ * rsc_make_pulse forms in RSC_PULSE_PLAIN mode.  Work is queued on `stream`
+ * (a cudaStream_t, NULL for the default stream); the call does not wait.
+ *
+ * The scratch the kernel needs (block partials, completion counter, gate
+ * origins, the weight tables) lives in one fixed __device__ array in the
+ * library instead of in memory the call allocates: every GPU that loads the
+ * library holds about 1.3 MB for it until the process exits.  The first call
+ * on a device looks the array's address up (once per device, with that
+ * device current); make that first call before any stream capture.  All calls
+ * share the one array and it keeps the contents of the last call (the counter
+ * is cleared at each call): two calls whose work overlaps on the GPU race, so
+ * order them on one stream or synchronise between them.  Sizes above the
+ * RSC_NOALLOC_* limits return RSC_ERR_ARG with a message naming the limit.
+ * No cudaMalloc, cudaFree or other allocating call is made. */
+int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scats, const float *range_weight,
+                           uint32_t range_n, const float range_desc[4], const float *angular_weight,
+                           uint32_t angular_n, const float angular_desc[4], float range_start, float range_delta,
+                           uint32_t range_count, const float sim_desc[16], float *pulse4, void *stream);
+
 /* Diagnostics: evaluate the shared elementary functions (rsmath.h) on the
  * device; fn: 0 sin, 1 cos, 2 log, 3 log1p, 4 acos, 5 atan2(a, b), 6 exp,
  * 7 pow(a, b).  Host arrays of n floats. */

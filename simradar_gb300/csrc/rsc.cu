@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "../../include/rsc.h"
@@ -739,6 +740,149 @@ int rsc_launch_count(rsc_worker *w, uint64_t *count) {
 int rsc_get_stream(rsc_worker *w, void **stream) {
     if (w == nullptr || stream == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
     *stream = (void *)w->stream;
+    return RSC_OK;
+}
+
+/* ---- pulse formation that allocates nothing ---------------------------------
+ * The pulse kernel needs scratch memory beyond its inputs and outputs: one
+ * float4 per gate per block for the block partials, a completion counter, and
+ * the gate origins and weight tables in device memory.  rsc_make_pulse takes
+ * them from buffers rsc_worker_malloc allocated.  rsc_make_pulse_noalloc takes
+ * them from the fixed array below instead, so a caller that must not allocate
+ * device memory can still form a pulse from its own device buffers. */
+#define RSC_NA_PARTIALS_OFF 0
+#define RSC_NA_PARTIALS_BYTES ((size_t)RSC_NOALLOC_MAX_BLOCKS * RSC_NOALLOC_MAX_GATES * 16)
+#define RSC_NA_RK_OFF (RSC_NA_PARTIALS_OFF + RSC_NA_PARTIALS_BYTES)
+#define RSC_NA_RW_OFF (RSC_NA_RK_OFF + (size_t)RSC_NOALLOC_MAX_GATES * 4)
+#define RSC_NA_AW_OFF (RSC_NA_RW_OFF + (size_t)RSC_NOALLOC_MAX_RANGE_TABLE * 4)
+#define RSC_NA_COUNTER_OFF (RSC_NA_AW_OFF + (size_t)RSC_NOALLOC_MAX_ANGULAR_TABLE * 4)
+#define RSC_NA_BYTES (RSC_NA_COUNTER_OFF + 256)
+
+/* One copy per device that loads this library, held until the process exits.
+ * Host code only ever uses the address cudaGetSymbolAddress returns for it. */
+static __device__ __align__(256) unsigned char g_pulse_scratch[RSC_NA_BYTES];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_na_mu;
+void *g_na_addr[kNoAllocMaxDevices] = {nullptr};
+
+/* Device address of g_pulse_scratch on the current device, looked up once per
+ * device (the first call on each device does it, with that device current). */
+int noalloc_scratch(void **out) {
+    int dev = 0;
+    RSC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(RSC_ERR_UNSUPPORTED, "device %d", dev);
+    std::lock_guard<std::mutex> lock(g_na_mu);
+    if (g_na_addr[dev] == nullptr) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_pulse_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            return fail(RSC_ERR_CUDA, "cudaGetSymbolAddress(pulse scratch) on device %d: %s", dev,
+                        cudaGetErrorString(e));
+        }
+        g_na_addr[dev] = p;
+    }
+    *out = g_na_addr[dev];
+    return RSC_OK;
+}
+
+}  // namespace
+
+int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scats, const float *range_weight,
+                           uint32_t range_n, const float range_desc[4], const float *angular_weight,
+                           uint32_t angular_n, const float angular_desc[4], float range_start, float range_delta,
+                           uint32_t range_count, const float sim_desc[16], float *pulse4, void *stream) {
+    if (pos4 == nullptr || rcs4 == nullptr || pulse4 == nullptr || range_weight == nullptr ||
+        range_desc == nullptr || angular_weight == nullptr || angular_desc == nullptr || sim_desc == nullptr) {
+        return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: NULL argument");
+    }
+    if (num_scats == 0) return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: num_scats is 0");
+    if (range_count == 0 || range_count > RSC_NOALLOC_MAX_GATES) {
+        return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: range_count %u outside [1, %d]", range_count,
+                    RSC_NOALLOC_MAX_GATES);
+    }
+    if (range_n == 0 || range_n > RSC_NOALLOC_MAX_RANGE_TABLE) {
+        return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: range weight table of %u entries, limit %d", range_n,
+                    RSC_NOALLOC_MAX_RANGE_TABLE);
+    }
+    if (angular_n == 0 || angular_n > RSC_NOALLOC_MAX_ANGULAR_TABLE) {
+        return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: angular weight table of %u entries, limit %d", angular_n,
+                    RSC_NOALLOC_MAX_ANGULAR_TABLE);
+    }
+    if (!(range_desc[2] >= 0.0f) || (uint32_t)range_desc[2] >= range_n || !(angular_desc[2] >= 0.0f) ||
+        (uint32_t)angular_desc[2] >= angular_n) {
+        return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: table max index beyond its table");
+    }
+    if (!(fabsf(range_start) < INFINITY) || !(fabsf(range_delta) < INFINITY)) {
+        return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: range_start / range_delta not finite");
+    }
+    void *base = nullptr;
+    int s = noalloc_scratch(&base);
+    if (s) return s;
+    unsigned char *b = static_cast<unsigned char *>(base);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint32_t G = range_count;
+    /* gate origins: the FP32 running sum of make_pulse_pass_1 (rs.cl:1214) */
+    float rk[RSC_NOALLOC_MAX_GATES];
+    float r = range_start;
+    for (uint32_t k = 0; k < G; k++) {
+        rk[k] = r;
+        r = r + range_delta;
+    }
+    RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_RK_OFF, rk, G * sizeof(float), cudaMemcpyHostToDevice, st));
+    RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_RW_OFF, range_weight, range_n * sizeof(float), cudaMemcpyHostToDevice, st));
+    RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_AW_OFF, angular_weight, angular_n * sizeof(float), cudaMemcpyHostToDevice, st));
+    /* the counter must start at zero; the partials are written before read */
+    RSC_CUDA(cudaMemsetAsync(b + RSC_NA_COUNTER_OFF, 0, sizeof(unsigned), st));
+    /* launch geometry of the plain pulse kernel, capped to the scratch size */
+    int dev = 0, sms = 0, per_sm = 1;
+    RSC_CUDA(cudaGetDevice(&dev));
+    RSC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int threads = 16 * 32;
+    const size_t smem = (size_t)16 * G * 16 + 2 * G * sizeof(float);
+    RSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<0>, threads, smem));
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 4) per_sm = 4;
+    int grid = sms * per_sm;
+    if (grid > RSC_NOALLOC_MAX_BLOCKS) grid = RSC_NOALLOC_MAX_BLOCKS;
+    PulseArgs P;
+    memset(&P, 0, sizeof(P));
+    P.pos = reinterpret_cast<const float4 *>(pos4);
+    P.rcs = reinterpret_cast<const float4 *>(rcs4);
+    P.n = num_scats;
+    P.aw = reinterpret_cast<const float *>(b + RSC_NA_AW_OFF);
+    memcpy(P.awd, angular_desc, sizeof(P.awd));
+    P.rw = reinterpret_cast<const float *>(b + RSC_NA_RW_OFF);
+    memcpy(P.rwd, range_desc, sizeof(P.rwd));
+    P.rk = reinterpret_cast<const float *>(b + RSC_NA_RK_OFF);
+    P.G = G;
+    memcpy(P.sim, sim_desc, sizeof(P.sim));
+    P.rs = range_start;
+    P.inv_delta = range_delta != 0.0f ? 1.0f / range_delta : 0.0f;
+    P.partials = b + RSC_NA_PARTIALS_OFF;
+    P.counter = reinterpret_cast<unsigned *>(b + RSC_NA_COUNTER_OFF);
+    P.pulse = reinterpret_cast<float4 *>(pulse4);
+    /* sparse gate window when both edge weights are zero (see fill_pulse_args) */
+    P.dense = 1;
+    const float xs = range_desc[0], x0 = range_desc[1], xm = range_desc[2];
+    if (range_delta > 0.0f && xs > 0.0f && range_weight[0] == 0.0f && range_weight[(uint32_t)xm] == 0.0f) {
+        double d_lo = -(double)x0 / (double)xs, d_hi = ((double)xm - (double)x0) / (double)xs;
+        double drift = 0.0;
+        for (uint32_t k = 0; k < G; k++) {
+            drift = fmax(drift, fabs((double)rk[k] - ((double)range_start + (double)k * (double)range_delta)));
+        }
+        double margin = (drift + 1.0e-3 * fabs((double)range_delta)) / (double)range_delta + 0.05;
+        double lo = d_lo / (double)range_delta - margin, hi = d_hi / (double)range_delta + margin;
+        if (hi - lo + 1.0 < (double)rsc::kMaxCandidates) {
+            P.dense = 0;
+            P.win_lo = (float)lo;
+            P.win_hi = (float)hi;
+        }
+    }
+    rsc::k_pulse<0><<<grid, threads, smem, st>>>(P);
+    RSC_CUDA(cudaGetLastError());
     return RSC_OK;
 }
 
