@@ -16,7 +16,7 @@
 #include <vector>
 
 #include "../../include/rsc.h"
-#include "rsc_kernels.cuh"
+#include "rsc_pulse.cuh"
 
 using rsc::AdvanceArgs;
 using rsc::DebrisType;
@@ -230,8 +230,7 @@ int set_gates(rsc_worker *w) {
 }
 
 int pulse_geometry(rsc_worker *w, int mode, int *grid, int *threads, size_t *smem) {
-    size_t bin_bytes = (mode == RSC_PULSE_PLAIN) ? 16 : 32;  /* per gate per warp */
-    size_t per_warp = (size_t)w->G * bin_bytes;
+    size_t per_warp = rsc::pulse_warp_bytes(mode, w->G);
     size_t budget = 200 * 1024;
     int warps = (int)(budget / per_warp);
     if (warps > 16) warps = 16;
@@ -841,7 +840,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     RSC_CUDA(cudaGetDevice(&dev));
     RSC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int threads = 16 * 32;
-    const size_t smem = (size_t)16 * G * 16 + 2 * G * sizeof(float);
+    const size_t smem = 16 * rsc::pulse_warp_bytes(RSC_PULSE_PLAIN, G) + 2 * G * sizeof(float);
     RSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<0>, threads, smem));
     if (per_sm < 1) per_sm = 1;
     if (per_sm > 4) per_sm = 4;

@@ -5,16 +5,10 @@
  *                 background range and db_atts on every debris range
  *                 (rs.cl:533-907), one thread per scatterer, float4 loads.
  *   k_db_rcs      debris RCS refresh after a beam move (rs.cl:909-919).
- *   k_pulse       scat_sig_aux + make_pulse_pass_1 + make_pulse_pass_2
- *                 (rs.cl:1050-1441) fused: each scatterer's signal is formed
- *                 in registers and added only to the gates its range weight
- *                 reaches (the gate weights are the bit-exact pass-1 weights),
- *                 per-warp gate bins in shared memory, one partial per block,
- *                 and the last block to finish sums the partials in block
- *                 order.  Three precisions: plain FP32, compensated FP32
- *                 (double-float range, split phase, double-float sums), FP64.
  *   k_sig_aux     forms aux / sig for RS_download when the pulse kernel did
  *                 not write them.
+ * plus the pieces the pulse kernel (rsc_pulse.cuh) is built from: the
+ * pass-1 weights, the per-scatterer signal and the per-warp gate bins.
  */
 #ifndef SIMRADAR_GB300_RSC_KERNELS_CUH
 #define SIMRADAR_GB300_RSC_KERNELS_CUH
@@ -278,7 +272,10 @@ __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned lon
     return t;
 }
 
-__global__ void __launch_bounds__(kAdvanceThreads) k_advance(const AdvanceArgs a) {
+/* 6 blocks of 256 per SM (<= 42 registers): the step is a chain of dependent
+ * loads (state, then 8 LES texels, then the debris tables), so resident warps
+ * are what hides the latency */
+__global__ void __launch_bounds__(kAdvanceThreads, 6) k_advance(const AdvanceArgs a) {
     const unsigned b = blockIdx.x;
     if (b < a.rain_blocks) {
         unsigned long long j = (unsigned long long)b * kAdvanceThreads + threadIdx.x;
@@ -334,12 +331,14 @@ struct PulseArgs {
     double *pulse64;
 };
 
-/* the pass-1 weight of one gate (rs.cl:1196-1209), bit-exact */
+/* the pass-1 weight of one gate (rs.cl:1196-1209), bit-exact.  The clamp
+ * leaves an integer-valued floor in [0, max] (a NaN index clamps to 0), so
+ * the conversion needs no range check. */
 __device__ __forceinline__ float range_weight(const PulseArgs &P, float d) {
     float f0, f1;
     float dec0 = cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, P.rwd[2]), &f0);
     (void)cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 1.0f), 0.0f, P.rwd[2]), &f1);
-    return cl_mix(__ldg(P.rw + cl_f2u_rtz(f0)), __ldg(P.rw + cl_f2u_rtz(f1)), dec0);
+    return cl_mix(__ldg(P.rw + (uint32_t)f0), __ldg(P.rw + (uint32_t)f1), dec0);
 }
 
 /* the angular weight of scat_sig_aux (rs.cl:1066-1089) */
@@ -349,7 +348,7 @@ __device__ __forceinline__ float angular_weight(const PulseArgs &P, float angle)
     float raw1 = cl_clamp(fmaf(angle, P.awd[0], P.awd[1] + 1.0f), 0.0f, P.awd[2]);
     float dec0 = cl_fract(raw0, &fi0);
     (void)cl_fract(raw1, &fi1);
-    return cl_mix(__ldg(P.aw + cl_f2u_rtz(fi0)), __ldg(P.aw + cl_f2u_rtz(fi1)), dec0);
+    return cl_mix(__ldg(P.aw + (uint32_t)fi0), __ldg(P.aw + (uint32_t)fi1), dec0);
 }
 
 /* error-free transformations */
@@ -497,58 +496,6 @@ __device__ __forceinline__ void signal_plain(const PulseArgs &P, float4 p, float
     o.r_lo = 0.0f;
 }
 
-/* compensated: range as a double-float from the FP32 position, angle from a
- * well-conditioned atan2(|b x p|, b . p), phase k r reduced by pi/2 with the
- * product k * r_hi split exactly (fmaf) and the tails added after reduction */
-__device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4 x, Sig32 &o) {
-    const float *sd = P.sim;
-    float ax, ex, ay, ey, az, ez;
-    two_prod(p.x, p.x, ax, ex);
-    two_prod(p.y, p.y, ay, ey);
-    two_prod(p.z, p.z, az, ez);
-    float s1, e1, s2, e2;
-    two_sum(ax, ay, s1, e1);
-    two_sum(s1, az, s2, e2);
-    float lo = ((ex + ey) + ez) + (e1 + e2);
-    float sh = s2 + lo;
-    float sl = lo - (sh - s2);
-    float rh = sqrtf(sh);
-    float rl = (fmaf(-rh, rh, sh) + sl) / (2.0f * rh);
-    float r = rh + rl;
-    float r_lo = rl - (r - rh);
-    /* b x p with each product difference computed with one rounding */
-    const float bx = sd[0], by = sd[1], bz = sd[2];
-    float t, e;
-    two_prod(bz, p.y, t, e);
-    float cx = fmaf(by, p.z, -t) - e;
-    two_prod(bx, p.z, t, e);
-    float cy = fmaf(bz, p.x, -t) - e;
-    two_prod(by, p.x, t, e);
-    float cz = fmaf(bx, p.y, -t) - e;
-    float cn = sqrtf(cx * cx + cy * cy + cz * cz);
-    float dt = fmaf(bx, p.x, fmaf(by, p.y, bz * p.z));
-    float angle = rsm_atan2f(cn, dt);
-    o.wang = angular_weight(P, angle);
-    /* phase */
-    float ph, pl;
-    two_prod(sd[4], r, ph, pl);
-    pl = fmaf(sd[4], r_lo, pl);
-    float q;
-    float red = rsm_reduce_pio2(ph, &q);
-    red = red + pl;
-    float ss, cc;
-    rsm_sincos_reduced(red, q, &ss, &cc);
-    float atten = 1.0f / (r * r);
-    float ms = -ss;
-    o.sig[0] = (x.x * cc - x.y * ms) * atten;
-    o.sig[1] = (x.y * cc + x.x * ms) * atten;
-    o.sig[2] = (x.z * cc - x.w * ms) * atten;
-    o.sig[3] = (x.w * cc + x.z * ms) * atten;
-    o.s.set(o.sig[0] * o.wang, o.sig[1] * o.wang, o.sig[2] * o.wang, o.sig[3] * o.wang);
-    o.r = r;
-    o.r_lo = r_lo;
-}
-
 __device__ __forceinline__ bool finite4(const float *v) {
     return fabsf(v[0]) < INFINITY && fabsf(v[1]) < INFINITY && fabsf(v[2]) < INFINITY && fabsf(v[3]) < INFINITY;
 }
@@ -564,221 +511,6 @@ __device__ __forceinline__ double lerp64(const float *W, const float *desc, doub
     int i1 = (fl + 1.0 > m) ? (int)m : i0 + 1;
     double w0 = (double)__ldg(W + i0), w1 = (double)__ldg(W + i1);
     return w0 + (w1 - w0) * a;
-}
-
-template <int MODE>  /* RSC_PULSE_PLAIN, RSC_PULSE_COMPENSATED, RSC_PULSE_F64 */
-struct PulseTraits;
-template <> struct PulseTraits<0> { typedef AccF32 Acc; };
-template <> struct PulseTraits<1> { typedef AccDF Acc; };
-template <> struct PulseTraits<2> { typedef AccF64 Acc; };
-
-template <int MODE>
-__global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
-    typedef typename PulseTraits<MODE>::Acc Acc;
-    typedef typename Acc::bin_t bin_t;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned G = P.G;
-    const unsigned words = G * 4 * Acc::kWords;          /* bin_t per warp */
-    const unsigned nwarps = blockDim.x >> 5;
-    const unsigned warp = threadIdx.x >> 5;
-    const unsigned lane = threadIdx.x & 31u;
-    bin_t *bins = reinterpret_cast<bin_t *>(smem_raw);
-    float *rk_s = reinterpret_cast<float *>(bins + (size_t)nwarps * words);
-    float *rkl_s = rk_s + G;
-    for (unsigned t = threadIdx.x; t < nwarps * words; t += blockDim.x) bins[t] = (bin_t)0;
-    for (unsigned t = threadIdx.x; t < G; t += blockDim.x) {
-        rk_s[t] = P.rk[t];
-        rkl_s[t] = (MODE == 1) ? P.rk_lo[t] : 0.0f;
-    }
-    __syncthreads();
-    bin_t *wbins = bins + (size_t)warp * words;
-
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    const unsigned long long n = P.n;
-    /* every lane of a warp runs the same number of iterations so the warp
-     * collectives below see the full warp */
-    const unsigned long long base0 = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
-    for (unsigned long long base = base0; base < n; base += stride) {
-        const unsigned long long i = base + lane;
-        const bool in = i < n;
-        Acc c;
-        float r = 0.0f, r_lo = 0.0f;
-        double r64 = 0.0;
-        bool finite = false;
-        if (in) {
-            float4 p = __ldg(P.pos + i);
-            float4 x = __ldg(P.rcs + i);
-            if constexpr (MODE == 2) {
-                double px = p.x, py = p.y, pz = p.z;
-                r64 = sqrt(px * px + py * py + pz * pz);
-                double bx = P.sim[0], by = P.sim[1], bz = P.sim[2];
-                double cx = by * pz - bz * py, cy = bz * px - bx * pz, cz = bx * py - by * px;
-                double ang = atan2(sqrt(cx * cx + cy * cy + cz * cz), bx * px + by * py + bz * pz);
-                double wa = lerp64(P.aw, P.awd, ang);
-                double atten = 1.0 / (r64 * r64);
-                double ss, cc;
-                sincos((double)P.sim[4] * r64, &ss, &cc);
-                double k = atten * wa;
-                c.v[0] = ((double)x.x * cc + (double)x.y * ss) * k;
-                c.v[1] = ((double)x.y * cc - (double)x.x * ss) * k;
-                c.v[2] = ((double)x.z * cc + (double)x.w * ss) * k;
-                c.v[3] = ((double)x.w * cc - (double)x.z * ss) * k;
-                r = (float)r64;
-                finite = isfinite(r64) && isfinite(c.v[0]) && isfinite(c.v[1]) && isfinite(c.v[2]) &&
-                         isfinite(c.v[3]);
-            } else {
-                Sig32 sg;
-                if constexpr (MODE == 0) {
-                    signal_plain(P, p, x, sg);
-                } else {
-                    signal_comp(P, p, x, sg);
-                }
-                c.set(sg.s.v[0], sg.s.v[1], sg.s.v[2], sg.s.v[3]);
-                r = sg.r;
-                r_lo = sg.r_lo;
-                finite = fabsf(r) < INFINITY && finite4(sg.s.v);
-                if (MODE == 0 && P.materialize) {
-                    float4 ax = P.aux[i];
-                    ax.x = r;
-                    ax.y = ax.y + P.sim[15];
-                    ax.w = sg.wang;
-                    P.aux[i] = ax;
-                    P.sig[i] = make_float4(sg.sig[0], sg.sig[1], sg.sig[2], sg.sig[3]);
-                }
-            }
-        }
-        if (!P.dense) {
-            /* candidate gates: only those the range weight can reach */
-            int k_lo = 0, k_hi = -1;
-            if (in && finite) {
-                float g = (r - P.rs) * P.inv_delta;
-                k_lo = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
-                k_hi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
-            }
-            const int maxc = min(kMaxCandidates, (int)__reduce_max_sync(0xffffffffu, (unsigned)max(k_hi - k_lo + 1, 0)));
-            for (int j = 0; j < maxc; j++) {
-                const int gate = k_lo + j;
-                bool valid = gate <= k_hi;
-                Acc cw;
-                if (valid) {
-                    if constexpr (MODE == 2) {
-                        double w = lerp64(P.rw, P.rwd, r64 - P.rk64[gate]);
-                        c.scale(w, cw);
-                        valid = (w != 0.0);
-                    } else {
-                        float d = (MODE == 1) ? (r - rk_s[gate]) + (r_lo - rkl_s[gate]) : r - rk_s[gate];
-                        float w = range_weight(P, d);
-                        c.scale(w, cw);
-                        valid = (w != 0.0f);
-                    }
-                }
-                bin_add<Acc>(wbins, 0xffffffffu, valid, gate, cw);
-            }
-            /* a non-finite signal meets every gate (0 * inf = NaN in pass 1) */
-            if (__any_sync(0xffffffffu, in && !finite)) {
-                for (unsigned k = 0; k < G; k++) {
-                    bool valid = in && !finite;
-                    Acc cw;
-                    if (valid) {
-                        if constexpr (MODE == 2) {
-                            c.scale(lerp64(P.rw, P.rwd, r64 - P.rk64[k]), cw);
-                        } else {
-                            c.scale(range_weight(P, r - rk_s[k]), cw);
-                        }
-                    }
-                    bin_add<Acc>(wbins, 0xffffffffu, valid, (int)k, cw);
-                }
-            }
-        } else {
-            /* dense: every gate, as pass 1 does; the warp sums each gate with a
-             * fixed shuffle tree and lane 0 adds it to the warp's bin */
-            for (unsigned k = 0; k < G; k++) {
-                Acc cw;
-                cw.set(0, 0, 0, 0);
-                if (in) {
-                    if constexpr (MODE == 2) {
-                        c.scale(lerp64(P.rw, P.rwd, r64 - P.rk64[k]), cw);
-                    } else {
-                        float d = (MODE == 1) ? (r - rk_s[k]) + (r_lo - rkl_s[k]) : r - rk_s[k];
-                        c.scale(range_weight(P, d), cw);
-                    }
-                }
-                warp_sum_into<Acc>(wbins + (size_t)k * 4 * Acc::kWords, cw);
-            }
-        }
-    }
-    __syncthreads();
-
-    /* block partial: warp bins summed in warp order */
-    const unsigned outs = G * 4;
-    bin_t *part = reinterpret_cast<bin_t *>(P.partials) + (size_t)blockIdx.x * outs * Acc::kWords;
-    for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
-        const unsigned k = o >> 2, l = o & 3u;
-        if (Acc::kWords == 2) {
-            float hi = 0.0f, lo = 0.0f;
-            for (unsigned wv = 0; wv < nwarps; wv++) {
-                const float *b = reinterpret_cast<const float *>(bins) + (size_t)wv * words + k * 8;
-                float s, e;
-                two_sum(hi, b[l], s, e);
-                hi = s;
-                lo = lo + (e + b[4 + l]);
-            }
-            reinterpret_cast<float *>(part)[o] = hi;
-            reinterpret_cast<float *>(part)[outs + o] = lo;
-        } else {
-            bin_t acc = (bin_t)0;
-            for (unsigned wv = 0; wv < nwarps; wv++) acc = acc + bins[(size_t)wv * words + o];
-            part[o] = acc;
-        }
-    }
-    __threadfence();
-    __syncthreads();
-    __shared__ bool s_last;
-    if (threadIdx.x == 0) {
-        unsigned ticket = atomicAdd(P.counter, 1u);
-        s_last = (ticket == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    /* last block: sum the block partials in block order; warp w takes
-     * outputs w, w + nwarps, ...; lanes stride over blocks, then a fixed
-     * shuffle tree */
-    const unsigned nb = gridDim.x;
-    for (unsigned o = warp; o < outs; o += nwarps) {
-        if (Acc::kWords == 2) {
-            const float *pf = reinterpret_cast<const float *>(P.partials);
-            float hi = 0.0f, lo = 0.0f;
-            for (unsigned b = lane; b < nb; b += 32) {
-                const float *pb = pf + (size_t)b * outs * 2;
-                float s, e;
-                two_sum(hi, __ldcg(pb + o), s, e);
-                hi = s;
-                lo = lo + (e + __ldcg(pb + outs + o));
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                float ohi = __shfl_down_sync(0xffffffffu, hi, off);
-                float olo = __shfl_down_sync(0xffffffffu, lo, off);
-                float s, e;
-                two_sum(hi, ohi, s, e);
-                hi = s;
-                lo = lo + (e + olo);
-            }
-            if (lane == 0) reinterpret_cast<float *>(P.pulse)[o] = hi + lo;
-        } else {
-            const bin_t *pf = reinterpret_cast<const bin_t *>(P.partials);
-            bin_t acc = (bin_t)0;
-            for (unsigned b = lane; b < nb; b += 32) acc = acc + __ldcg(pf + (size_t)b * outs + o);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, off);
-            if (lane == 0) {
-                reinterpret_cast<float *>(P.pulse)[o] = (float)acc;
-                if (MODE == 2) P.pulse64[o] = (double)acc;
-            }
-        }
-    }
-    if (threadIdx.x == 0) *P.counter = 0u;
 }
 
 /* scat_sig_aux (rs.cl:1050-1110) for RS_download */

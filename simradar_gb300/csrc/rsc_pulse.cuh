@@ -1,0 +1,437 @@
+/*
+ * rsc_pulse.cuh -- pulse formation on sm_103a: scat_sig_aux, make_pulse_pass_1
+ * and make_pulse_pass_2 (rs.cl:1050-1441) as one kernel.
+ *
+ * Each thread forms its scatterer's signal in registers and adds it only to the
+ * gates the range weight can reach (the weights are the pass-1 weights, bit for
+ * bit).  Sums go into per-warp gate bins in shared memory; each block writes one
+ * partial per gate and the last block to finish adds the partials in block
+ * order, so the pulse comes out of a single launch.
+ *
+ *   RSC_PULSE_PLAIN        FP32 throughout, as the reference; per-warp bins
+ *                          updated with shared-memory atomics.
+ *   RSC_PULSE_COMPENSATED  range, beam angle and gate offsets as double-floats,
+ *                          split range phase, FP64 gate origins, table indices
+ *                          with their rounding error carried; contributions go
+ *                          into FP32 per-warp bins that the warp folds into
+ *                          double-float bins after every 32 scatterers, and the
+ *                          block and grid sums stay double-float.
+ *   RSC_PULSE_F64          FP64 reference of the same FP32 state: per-warp
+ *                          FP64 bins, lanes on the same gate serialised.
+ *
+ * Bins of FP32 sums are 5 floats apart per gate so that lanes on different
+ * gates rarely meet in one shared-memory bank (5 is prime to the 32 banks).
+ */
+#ifndef SIMRADAR_GB300_RSC_PULSE_CUH
+#define SIMRADAR_GB300_RSC_PULSE_CUH
+
+#include "rsc_kernels.cuh"
+
+namespace rsc {
+
+constexpr unsigned kBinStride32 = 5;   /* floats per gate in an FP32 bin row */
+
+/* Table lerp at index (a_hi + a_lo) * desc[0] + desc[1], clamped to
+ * [0, desc[2]], with the rounding error of the index computation carried into
+ * the interpolation fraction (compensated form). */
+__device__ __forceinline__ float weight_comp(const float *W, const float *desc, float a_hi, float a_lo) {
+    const float s = desc[0], o = desc[1], m = desc[2];
+    float p = a_hi * s;
+    float pe = fmaf(a_hi, s, -p) + a_lo * s;
+    float f, fe;
+    two_sum(p, o, f, fe);
+    fe = fe + pe;
+    const float fsum = f + fe;
+    if (!(fsum > 0.0f)) return __ldg(W);
+    if (fsum >= m) return __ldg(W + (int)m);
+    const float fl = floorf(fsum);
+    float frac = fminf(fmaxf((f - fl) + fe, 0.0f), 1.0f);
+    const int i0 = (int)fl;
+    const int i1 = min(i0 + 1, (int)m);
+    const float w0 = __ldg(W + i0), w1 = __ldg(W + i1);
+    return fmaf(w1 - w0, frac, w0);
+}
+
+/* double-float helpers: (hi, lo) with |lo| <= ulp(hi) / 2 */
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float &h, float &l) {
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e = e + (al + bl);
+    h = s + e;
+    l = e - (h - s);
+}
+__device__ __forceinline__ void df_sqrt(float ah, float al, float &h, float &l) {
+    float r = sqrtf(ah);
+    float c = (fmaf(-r, r, ah) + al) / (2.0f * r);
+    h = r + c;
+    l = c - (h - r);
+}
+__device__ __forceinline__ void df_div(float ah, float al, float bh, float bl, float &h, float &l) {
+    float q = ah / bh;
+    float c = (fmaf(-q, bh, ah) + al - q * bl) / bh;
+    h = q + c;
+    l = c - (h - q);
+}
+/* a * b exactly as a double-float, minus c * d exactly as a double-float */
+__device__ __forceinline__ void df_prod_diff(float a, float b, float c, float d, float &h, float &l) {
+    float p, pe, q, qe;
+    two_prod(a, b, p, pe);
+    two_prod(c, d, q, qe);
+    df_add(p, pe, -q, -qe, h, l);
+}
+/* sum of squares of three double-floats (the squares of the tails dropped) */
+__device__ __forceinline__ void df_norm2(const float *h3, const float *l3, float &h, float &l) {
+    float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float p, pe;
+        two_prod(h3[i], h3[i], p, pe);
+        pe = fmaf(2.0f * h3[i], l3[i], pe);
+        df_add(sh, sl, p, pe, sh, sl);
+    }
+    h = sh;
+    l = sl;
+}
+
+/* compensated signal.  Range r = |p| and the beam angle are double-floats
+ * from the FP32 position: the angle is asin(|b x p| / (|b| |p|)) with the
+ * cross product formed exactly (two_prod) and the asin series (rsmath.h)
+ * applied to the small correction only, so its error stays near 1e-12 where
+ * the antenna table can see it (< 15.5 deg).  The phase k r is reduced by
+ * pi/2 with k * r_hi split exactly and the tails added after reduction. */
+__device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4 x, Sig32 &o) {
+    const float *sd = P.sim;
+    /* range */
+    const float ph3[3] = {p.x, p.y, p.z}, pl3[3] = {0.0f, 0.0f, 0.0f};
+    float r2h, r2l, rh, rl;
+    df_norm2(ph3, pl3, r2h, r2l);
+    df_sqrt(r2h, r2l, rh, rl);
+    /* sin of the beam angle */
+    const float bx = sd[0], by = sd[1], bz = sd[2];
+    float ch[3], cl[3];
+    df_prod_diff(by, p.z, bz, p.y, ch[0], cl[0]);
+    df_prod_diff(bz, p.x, bx, p.z, ch[1], cl[1]);
+    df_prod_diff(bx, p.y, by, p.x, ch[2], cl[2]);
+    float c2h, c2l, cnh, cnl;
+    df_norm2(ch, cl, c2h, c2l);
+    df_sqrt(c2h, c2l, cnh, cnl);
+    const float bh3[3] = {bx, by, bz};
+    float b2h, b2l, bnh, bnl;
+    df_norm2(bh3, pl3, b2h, b2l);
+    df_sqrt(b2h, b2l, bnh, bnl);
+    float dph, dpl;                      /* |b| |p| */
+    two_prod(bnh, rh, dph, dpl);
+    dpl = fmaf(bnh, rl, fmaf(bnl, rh, dpl));
+    float sh, sl;
+    df_div(cnh, cnl, dph, dpl, sh, sl);
+    const float dot = fmaf(bx, p.x, fmaf(by, p.y, bz * p.z));
+    float ang_h, ang_l;
+    if (dot > 0.0f && sh < 0.5f) {
+        /* asin(s) = s + s z P(z): the P term is < 2% of s, float is enough */
+        const float z = sh * sh;
+        const float corr = rsm_asin_core(sh, z) - sh;
+        df_add(sh, sl, corr, 0.0f, ang_h, ang_l);
+    } else {
+        /* beyond 30 degrees (or behind the radar) the antenna table has
+         * clamped to its last entry long before */
+        ang_h = dot > 0.0f ? rsm_atan2f(cnh, dot) : RSC_PI_F;
+        ang_l = 0.0f;
+    }
+    o.wang = weight_comp(P.aw, P.awd, ang_h, ang_l);
+    /* phase */
+    float phh, phl;
+    two_prod(sd[4], rh, phh, phl);
+    phl = fmaf(sd[4], rl, phl);
+    float q;
+    float red = rsm_reduce_pio2(phh, &q);
+    red = red + phl;
+    float ss, cc;
+    rsm_sincos_reduced(red, q, &ss, &cc);
+    /* attenuation 1 / r^2 from the double-float r^2 */
+    const float inv = 1.0f / r2h;
+    const float atten = fmaf(-inv, r2l * inv, inv);
+    const float ms = -ss;
+    o.sig[0] = fmaf(x.x, cc, -(x.y * ms)) * atten;
+    o.sig[1] = fmaf(x.y, cc, x.x * ms) * atten;
+    o.sig[2] = fmaf(x.z, cc, -(x.w * ms)) * atten;
+    o.sig[3] = fmaf(x.w, cc, x.z * ms) * atten;
+    o.s.set(o.sig[0] * o.wang, o.sig[1] * o.wang, o.sig[2] * o.wang, o.sig[3] * o.wang);
+    o.r = rh;
+    o.r_lo = rl;
+}
+
+template <int MODE>  /* RSC_PULSE_PLAIN, RSC_PULSE_COMPENSATED, RSC_PULSE_F64 */
+struct PulseTraits;
+template <> struct PulseTraits<0> { typedef AccF32 Acc; static constexpr unsigned kMain = kBinStride32; };
+template <> struct PulseTraits<1> { typedef AccDF Acc; static constexpr unsigned kMain = 8; };
+template <> struct PulseTraits<2> { typedef AccF64 Acc; static constexpr unsigned kMain = 4; };
+
+/* shared memory per warp of k_pulse<MODE>, in bytes, for G gates */
+__host__ __device__ constexpr size_t pulse_warp_bytes(int mode, unsigned G) {
+    return mode == 0 ? (size_t)G * kBinStride32 * 4
+                     : (mode == 1 ? (size_t)G * (32 + kBinStride32 * 4) : (size_t)G * 32);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
+    typedef PulseTraits<MODE> Tr;
+    typedef typename Tr::Acc Acc;
+    typedef typename Acc::bin_t bin_t;
+    constexpr unsigned kMain = Tr::kMain;                /* bin_t per gate in the main bins */
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned G = P.G;
+    const unsigned words = G * kMain;
+    const unsigned nwarps = blockDim.x >> 5;
+    const unsigned warp = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    bin_t *bins = reinterpret_cast<bin_t *>(smem_raw);
+    float *mini_all = reinterpret_cast<float *>(bins + (size_t)nwarps * words);   /* compensated: FP32 mini bins */
+    for (unsigned t = threadIdx.x; t < nwarps * words; t += blockDim.x) bins[t] = (bin_t)0;
+    if (MODE == 1) {
+        for (unsigned t = threadIdx.x; t < nwarps * G * kBinStride32; t += blockDim.x) mini_all[t] = 0.0f;
+    }
+    __syncthreads();
+    bin_t *wbins = bins + (size_t)warp * words;
+    float *mini = mini_all + (size_t)warp * G * kBinStride32;
+    float *fbins = (MODE == 1) ? mini : reinterpret_cast<float *>(wbins);   /* where FP32 atomics go */
+
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long n = P.n;
+    /* every lane of a warp runs the same number of iterations so the warp
+     * collectives below see the full warp */
+    const unsigned long long base0 = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    for (unsigned long long base = base0; base < n; base += stride) {
+        const unsigned long long i = base + lane;
+        const bool in = i < n;
+        Acc c;
+        c.set(0, 0, 0, 0);
+        float r = 0.0f, r_lo = 0.0f;
+        double r64 = 0.0;
+        bool finite = false;
+        if (in) {
+            float4 p = __ldg(P.pos + i);
+            float4 x = __ldg(P.rcs + i);
+            if constexpr (MODE == 2) {
+                double px = p.x, py = p.y, pz = p.z;
+                r64 = sqrt(px * px + py * py + pz * pz);
+                double bx = P.sim[0], by = P.sim[1], bz = P.sim[2];
+                double cx = by * pz - bz * py, cy = bz * px - bx * pz, cz = bx * py - by * px;
+                double ang = atan2(sqrt(cx * cx + cy * cy + cz * cz), bx * px + by * py + bz * pz);
+                double wa = lerp64(P.aw, P.awd, ang);
+                double atten = 1.0 / (r64 * r64);
+                double ss, cc;
+                sincos((double)P.sim[4] * r64, &ss, &cc);
+                double k = atten * wa;
+                c.v[0] = ((double)x.x * cc + (double)x.y * ss) * k;
+                c.v[1] = ((double)x.y * cc - (double)x.x * ss) * k;
+                c.v[2] = ((double)x.z * cc + (double)x.w * ss) * k;
+                c.v[3] = ((double)x.w * cc - (double)x.z * ss) * k;
+                r = (float)r64;
+                finite = isfinite(r64) && isfinite(c.v[0]) && isfinite(c.v[1]) && isfinite(c.v[2]) &&
+                         isfinite(c.v[3]);
+            } else {
+                Sig32 sg;
+                if constexpr (MODE == 0) {
+                    signal_plain(P, p, x, sg);
+                } else {
+                    signal_comp(P, p, x, sg);
+                }
+                c.set(sg.s.v[0], sg.s.v[1], sg.s.v[2], sg.s.v[3]);
+                r = sg.r;
+                r_lo = sg.r_lo;
+                finite = fabsf(r) < INFINITY && finite4(sg.s.v);
+                if (MODE == 0 && P.materialize) {
+                    float4 ax = P.aux[i];
+                    ax.x = r;
+                    ax.y = ax.y + P.sim[15];
+                    ax.w = sg.wang;
+                    P.aux[i] = ax;
+                    P.sig[i] = make_float4(sg.sig[0], sg.sig[1], sg.sig[2], sg.sig[3]);
+                }
+            }
+        }
+        if (!P.dense) {
+            /* candidate gates: only those the range weight can reach */
+            int k_lo = 0, k_hi = -1;
+            if (in && finite) {
+                float g = (r - P.rs) * P.inv_delta;
+                k_lo = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
+                k_hi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
+            }
+            const int maxc = min(kMaxCandidates, (int)__reduce_max_sync(0xffffffffu, (unsigned)max(k_hi - k_lo + 1, 0)));
+            if constexpr (MODE == 2) {
+                for (int j = 0; j < maxc; j++) {
+                    const int gate = k_lo + j;
+                    Acc cw;
+                    bool nz = false;
+                    if (gate <= k_hi) {
+                        double w = lerp64(P.rw, P.rwd, r64 - P.rk64[gate]);
+                        c.scale(w, cw);
+                        nz = (w != 0.0);
+                    }
+                    bin_add<Acc>(wbins, 0xffffffffu, nz, gate, cw);
+                }
+            } else {
+                /* weights first (gate origins from global memory: they do not
+                 * alias the shared-memory bins), then the atomic adds */
+                float w[kMaxCandidates];
+#pragma unroll
+                for (int j = 0; j < kMaxCandidates; j++) {
+                    const int gate = k_lo + j;
+                    w[j] = 0.0f;
+                    if (j < maxc && gate <= k_hi) {
+                        if constexpr (MODE == 1) {
+                            w[j] = weight_comp(P.rw, P.rwd, r - __ldg(P.rk + gate), r_lo - __ldg(P.rk_lo + gate));
+                        } else {
+                            w[j] = range_weight(P, r - __ldg(P.rk + gate));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < kMaxCandidates; j++) {
+                    if (w[j] != 0.0f) {
+                        float *b = fbins + (size_t)(k_lo + j) * kBinStride32;
+                        atomicAdd(b + 0, w[j] * c.v[0]);
+                        atomicAdd(b + 1, w[j] * c.v[1]);
+                        atomicAdd(b + 2, w[j] * c.v[2]);
+                        atomicAdd(b + 3, w[j] * c.v[3]);
+                    }
+                }
+            }
+            /* a non-finite signal meets every gate (0 * inf = NaN in pass 1) */
+            if (__any_sync(0xffffffffu, in && !finite)) {
+                for (unsigned k = 0; k < G; k++) {
+                    bool valid = in && !finite;
+                    Acc cw;
+                    cw.set(0, 0, 0, 0);
+                    if (valid) {
+                        if constexpr (MODE == 2) {
+                            c.scale(lerp64(P.rw, P.rwd, r64 - P.rk64[k]), cw);
+                        } else {
+                            c.scale(range_weight(P, r - __ldg(P.rk + k)), cw);
+                        }
+                    }
+                    if constexpr (MODE == 2) {
+                        bin_add<Acc>(wbins, 0xffffffffu, valid, (int)k, cw);
+                    } else if (valid) {
+                        float *b = fbins + (size_t)k * kBinStride32;
+                        atomicAdd(b + 0, cw.v[0]);
+                        atomicAdd(b + 1, cw.v[1]);
+                        atomicAdd(b + 2, cw.v[2]);
+                        atomicAdd(b + 3, cw.v[3]);
+                    }
+                }
+            }
+        } else {
+            /* dense: every gate, as pass 1 does; the warp sums each gate with a
+             * fixed shuffle tree and lane 0 adds it to the warp's bin */
+            for (unsigned k = 0; k < G; k++) {
+                Acc cw;
+                cw.set(0, 0, 0, 0);
+                if (in) {
+                    if constexpr (MODE == 2) {
+                        c.scale(lerp64(P.rw, P.rwd, r64 - P.rk64[k]), cw);
+                    } else if constexpr (MODE == 1) {
+                        c.scale(weight_comp(P.rw, P.rwd, r - __ldg(P.rk + k), r_lo - __ldg(P.rk_lo + k)), cw);
+                    } else {
+                        c.scale(range_weight(P, r - __ldg(P.rk + k)), cw);
+                    }
+                }
+                warp_sum_into<Acc>(wbins + (size_t)k * kMain, cw);
+            }
+        }
+        if constexpr (MODE == 1) {
+            /* fold the FP32 mini bins into the warp's double-float bins */
+            __syncwarp();
+            float *df = reinterpret_cast<float *>(wbins);
+            for (unsigned o = lane; o < G * 4; o += 32) {
+                const unsigned k = o >> 2, l = o & 3u;
+                const float v = mini[k * kBinStride32 + l];
+                if (v != 0.0f) {
+                    float s, e;
+                    two_sum(df[k * 8 + l], v, s, e);
+                    df[k * 8 + l] = s;
+                    df[k * 8 + 4 + l] = df[k * 8 + 4 + l] + e;
+                    mini[k * kBinStride32 + l] = 0.0f;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+
+    /* block partial: warp bins summed in warp order */
+    const unsigned outs = G * 4;
+    bin_t *part = reinterpret_cast<bin_t *>(P.partials) + (size_t)blockIdx.x * outs * Acc::kWords;
+    for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
+        const unsigned k = o >> 2, l = o & 3u;
+        if constexpr (Acc::kWords == 2) {
+            float hi = 0.0f, lo = 0.0f;
+            for (unsigned wv = 0; wv < nwarps; wv++) {
+                const float *b = reinterpret_cast<const float *>(bins) + (size_t)wv * words + k * 8;
+                float s, e;
+                two_sum(hi, b[l], s, e);
+                hi = s;
+                lo = lo + (e + b[4 + l]);
+            }
+            reinterpret_cast<float *>(part)[o] = hi;
+            reinterpret_cast<float *>(part)[outs + o] = lo;
+        } else {
+            bin_t acc = (bin_t)0;
+            for (unsigned wv = 0; wv < nwarps; wv++) acc = acc + bins[(size_t)wv * words + k * kMain + l];
+            part[o] = acc;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        unsigned ticket = atomicAdd(P.counter, 1u);
+        s_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    /* last block: sum the block partials in block order; warp w takes
+     * outputs w, w + nwarps, ...; lanes stride over blocks, then a fixed
+     * shuffle tree */
+    const unsigned nb = gridDim.x;
+    for (unsigned o = warp; o < outs; o += nwarps) {
+        if constexpr (Acc::kWords == 2) {
+            const float *pf = reinterpret_cast<const float *>(P.partials);
+            float hi = 0.0f, lo = 0.0f;
+            for (unsigned b = lane; b < nb; b += 32) {
+                const float *pb = pf + (size_t)b * outs * 2;
+                float s, e;
+                two_sum(hi, __ldcg(pb + o), s, e);
+                hi = s;
+                lo = lo + (e + __ldcg(pb + outs + o));
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                float ohi = __shfl_down_sync(0xffffffffu, hi, off);
+                float olo = __shfl_down_sync(0xffffffffu, lo, off);
+                float s, e;
+                two_sum(hi, ohi, s, e);
+                hi = s;
+                lo = lo + (e + olo);
+            }
+            if (lane == 0) reinterpret_cast<float *>(P.pulse)[o] = hi + lo;
+        } else {
+            const bin_t *pf = reinterpret_cast<const bin_t *>(P.partials);
+            bin_t acc = (bin_t)0;
+            for (unsigned b = lane; b < nb; b += 32) acc = acc + __ldcg(pf + (size_t)b * outs + o);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, off);
+            if (lane == 0) {
+                reinterpret_cast<float *>(P.pulse)[o] = (float)acc;
+                if (MODE == 2) P.pulse64[o] = (double)acc;
+            }
+        }
+    }
+    if (threadIdx.x == 0) *P.counter = 0u;
+}
+
+}  // namespace rsc
+
+#endif

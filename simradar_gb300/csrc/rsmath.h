@@ -125,18 +125,15 @@ RSM_FN void rsm_sincos_reduced(float r, float q, float *s_out, float *c_out) {
     pc = fmaf(pc, z, 0x1.555556p-5f);            /*  1/24      */
     pc = fmaf(pc, z, (-0.5f));
     float cs = fmaf(z, pc, 1.0f);
-    /* quadrant from the low two bits of q (q is an integer-valued float) */
+    /* quadrant from the low two bits of q (q is an integer-valued float):
+     * (sin, cos) of r + quad pi/2 = (sn, cs), (cs, -sn), (-sn, -cs), (-cs, sn) */
     float q4 = q - 4.0f * floorf(q * 0.25f);
     int quad = (int)q4;
-    float s, c;
-    switch (quad & 3) {
-        case 0: s = sn; c = cs; break;
-        case 1: s = cs; c = -sn; break;
-        case 2: s = -sn; c = -cs; break;
-        default: s = -cs; c = sn; break;
-    }
-    *s_out = s;
-    *c_out = c;
+    const int swap = quad & 1;
+    float s = swap ? cs : sn;
+    float c = swap ? sn : cs;
+    *s_out = (quad & 2) ? -s : s;
+    *c_out = ((quad + 1) & 2) ? -c : c;
 }
 
 /* sin and cos of x.  Accurate for |x| < 6.7e6; beyond that the reduction

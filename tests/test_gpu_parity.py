@@ -117,13 +117,24 @@ def test_advance_concepts_bitexact(backend, oracle_lib, scene_db, concept):
 
 
 def test_pulse_plain_matches_oracle(backend, oracle_lib, scene_db):
-    W, st, pulses = run_pair(backend, oracle_lib, scene_db, 4, check_each=False)
-    for k, (g, r, r64, ab) in enumerate(pulses):
+    """Against the reference's own summation order (pass 1 + pass 2) and
+    against the exact sum of the same FP32 contributions."""
+    S = scene_db
+    O = oracle_lib
+    pop = synth.population(S)
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    st = O.OracleState(S.state)
+    for k in range(4):
+        sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+        W.make_pulse(sd)
+        g = W.download_pulse(1.0)
         assert np.isfinite(g).all()
-        lim = PULSE_TOL * ab + 1e-30
-        bad = np.abs(g.astype(np.float64) - r) > lim
-        assert not bad.any(), "pulse %d: %d of %d values beyond tolerance, worst ratio %g" % (
-            k, bad.sum(), bad.size, (np.abs(g - r) / lim).max())
+        direct, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+        assert_pulse_close(g, O.make_pulse(st, S, sd), ab, "pulse %d vs reference order" % k)
+        assert_pulse_close(g, direct, ab, "pulse %d vs exact sum" % k)
+        W.advance_time(pop, 0, sd)
+        O.advance_time(st, S, S.counts, S.les[0], sd)
     W.close()
 
 

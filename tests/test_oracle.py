@@ -168,3 +168,38 @@ def test_pass2_bodies_agree(oracle_lib):
         assert np.all(np.abs(p - ref) <= 5e-3 * ab + 1e-30)
     for p in outs[1:]:
         assert np.all(np.abs(p - outs[0]) <= 5e-5 * ab + 1e-30)
+
+
+def test_reference_order_matches_exact_sum(oracle_lib):
+    """pass 1 + pass 2 in the reference's order equals the exact sum of its own
+    FP32 contributions within the FP32 reordering bound, for the plan sizes
+    the reference runs (power-of-two work groups)."""
+    O = oracle_lib
+    from simradar_gb300 import synth
+    for n in (128, 4096, 131072):
+        S = synth.make_scene(num_rain=n, les_count=1)
+        st = O.OracleState(S.state)
+        sd = synth.pulse_sim_desc(S, 7)
+        p = O.make_pulse(st, S, sd)
+        direct, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+        assert np.all(np.abs(p - direct) <= 2e-5 * ab + 1e-30), n
+
+
+def test_reference_tree_quirk_below_128(oracle_lib):
+    """With 62 scatterers the pass-1 work group is 31 wide and the reference's
+    tree reduction (rs.cl:1224-1290) folds entries of the next gate's column
+    into a gate: its pulse then differs from the exact sum of its own
+    contributions, and the backend follows the exact sum."""
+    O = oracle_lib
+    from simradar_gb300 import synth
+    assert not O.reference_plan_valid(62) and O.reference_plan_valid(64)
+    S = synth.make_scene(num_rain=62, les_count=1)
+    st = O.OracleState(S.state)
+    # point the beam at the scatterers so the sums are not negligible
+    p = S.state["pos"][:, :3].astype(np.float64).mean(axis=0)
+    sd = S.sim_desc.copy()
+    sd[0:3] = (p / np.linalg.norm(p)).astype(np.float32)
+    ref = O.make_pulse(st, S, sd)
+    direct, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+    assert np.any(np.abs(ref - direct) > 1e-3 * ab + 1e-30)
+    assert O.lib().or_make_pulse_params.restype is not None
