@@ -172,9 +172,8 @@ int rsc_launch_count(rsc_worker *w, uint64_t *count);
 int rsc_get_stream(rsc_worker *w, void **stream);
 
 /* Limits of rsc_make_pulse_noalloc (its scratch is a fixed device array of
- * about 1.3 MB per GPU that loads this library). */
+ * about 9 KB per GPU that loads this library). */
 #define RSC_NOALLOC_MAX_GATES 128
-#define RSC_NOALLOC_MAX_BLOCKS 640
 #define RSC_NOALLOC_MAX_RANGE_TABLE 64
 #define RSC_NOALLOC_MAX_ANGULAR_TABLE 1024
 
@@ -192,14 +191,15 @@ int rsc_get_stream(rsc_worker *w, void **stream);
  * rsc_make_pulse forms in RSC_PULSE_PLAIN mode.  Work is queued on `stream`
  * (a cudaStream_t, NULL for the default stream); the call does not wait.
  *
- * The scratch the kernel needs (block partials, completion counter, gate
- * origins, the weight tables) lives in one fixed __device__ array in the
- * library instead of in memory the call allocates: every GPU that loads the
- * library holds about 1.3 MB for it until the process exits.  The first call
+ * The scratch the kernel needs (an FP64 accumulator per gate, a completion
+ * counter, gate origins, the weight tables) lives in one fixed __device__
+ * array in the library instead of in memory the call allocates: every GPU
+ * that loads the library holds about 9 KB for it until the process exits.
+ * The accumulator and the counter are cleared at each call.  The first call
  * on a device looks the array's address up (once per device, with that
  * device current); make that first call before any stream capture.  All calls
- * share the one array and it keeps the contents of the last call (the counter
- * is cleared at each call): two calls whose work overlaps on the GPU race, so
+ * share the one array and it keeps the contents of the last call: two calls
+ * whose work overlaps on the GPU race, so
  * order them on one stream or synchronise between them.  Sizes above the
  * RSC_NOALLOC_* limits return RSC_ERR_ARG with a message naming the limit.
  * No cudaMalloc, cudaFree or other allocating call is made. */

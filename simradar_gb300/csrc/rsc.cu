@@ -68,14 +68,14 @@ struct rsc_worker {
     double *pulse64 = nullptr;
     float *rk = nullptr, *rk_hi = nullptr, *rk_lo = nullptr;
     double *rk64 = nullptr;
-    void *partials = nullptr;
-    size_t partials_bytes = 0;
+    double *acc64 = nullptr;      /* the pulse kernel's FP64 grid accumulator */
     unsigned *counter = nullptr;
     /* tables */
     float *range_weight = nullptr;
     uint32_t range_n = 0;
     float range_desc[4] = {0};
     float range_weight_host0 = 1.0f, range_weight_hostm = 1.0f; /* edge values W[0], W[xm] */
+    float range_weight_small[4] = {0.0f, 0.0f, 0.0f, 0.0f};   /* the first 4 entries, for tables of <= 4 */
     float *angular_weight = nullptr;
     uint32_t angular_n = 0;
     float angular_desc[4] = {0};
@@ -134,14 +134,14 @@ void free_arrays(rsc_worker *w) {
     free_ptr(w->rk_hi);
     free_ptr(w->rk_lo);
     free_ptr(w->rk64);
-    free_ptr(w->partials);
+    free_ptr(w->acc64);
     free_ptr(w->counter);
     w->pos = w->vel = w->ori = w->tum = w->aux = w->rcs = w->sig = w->pulse = nullptr;
     w->rnd = nullptr;
     w->pulse64 = nullptr;
     w->rk = w->rk_hi = w->rk_lo = nullptr;
     w->rk64 = nullptr;
-    w->partials = nullptr;
+    w->acc64 = nullptr;
     w->counter = nullptr;
     w->num_scats = w->numel = 0;
 }
@@ -274,7 +274,10 @@ void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
     memcpy(P.sim, sim, sizeof(P.sim));
     P.rs = w->range_start;
     P.inv_delta = w->range_delta != 0.0f ? 1.0f / w->range_delta : 0.0f;
-    P.partials = w->partials;
+    P.rdelta = w->range_delta;
+    P.rw_n = w->range_n;
+    memcpy(P.rwv, w->range_weight_small, sizeof(P.rwv));
+    P.acc64 = w->acc64;
     P.counter = w->counter;
     P.pulse = w->pulse;
     P.pulse64 = w->pulse64;
@@ -403,9 +406,9 @@ int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float 
     RSC_CUDA(cudaMalloc((void **)&w->rk_hi, range_count * sizeof(float)));
     RSC_CUDA(cudaMalloc((void **)&w->rk_lo, range_count * sizeof(float)));
     RSC_CUDA(cudaMalloc((void **)&w->rk64, range_count * sizeof(double)));
-    /* block partials for the largest grid any precision uses (8 B per word) */
-    w->partials_bytes = (size_t)w->num_sms * 4 * range_count * 4 * 8;
-    RSC_CUDA(cudaMalloc(&w->partials, w->partials_bytes));
+    /* the pulse kernel's FP64 accumulator; each launch leaves it at zero */
+    RSC_CUDA(cudaMalloc((void **)&w->acc64, range_count * 4 * sizeof(double)));
+    RSC_CUDA(cudaMemsetAsync(w->acc64, 0, range_count * 4 * sizeof(double), w->stream));
     RSC_CUDA(cudaMalloc((void **)&w->counter, sizeof(unsigned)));
     RSC_CUDA(cudaMemsetAsync(w->counter, 0, sizeof(unsigned), w->stream));
     s = set_gates(w);
@@ -428,6 +431,7 @@ int rsc_set_range_weight(rsc_worker *w, const float *table, uint32_t n, const fl
     memcpy(w->range_desc, desc, sizeof(w->range_desc));
     w->range_weight_host0 = table[0];
     w->range_weight_hostm = table[(uint32_t)desc[2]];
+    for (uint32_t k = 0; k < 4; k++) w->range_weight_small[k] = k < n ? table[k] : 0.0f;
     return RSC_OK;
 }
 
@@ -672,8 +676,6 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     size_t smem = 0;
     s = pulse_geometry(w, mode, &grid, &threads, &smem);
     if (s) return s;
-    size_t need = (size_t)grid * w->G * 4 * 8;
-    if (need > w->partials_bytes) return fail(RSC_ERR_STATE, "partials buffer too small");
     PulseArgs P;
     fill_pulse_args(w, P, sim_desc);
     if (mode == RSC_PULSE_COMPENSATED) {
@@ -743,15 +745,15 @@ int rsc_get_stream(rsc_worker *w, void **stream) {
 }
 
 /* ---- pulse formation that allocates nothing ---------------------------------
- * The pulse kernel needs scratch memory beyond its inputs and outputs: one
- * float4 per gate per block for the block partials, a completion counter, and
- * the gate origins and weight tables in device memory.  rsc_make_pulse takes
- * them from buffers rsc_worker_malloc allocated.  rsc_make_pulse_noalloc takes
- * them from the fixed array below instead, so a caller that must not allocate
- * device memory can still form a pulse from its own device buffers. */
-#define RSC_NA_PARTIALS_OFF 0
-#define RSC_NA_PARTIALS_BYTES ((size_t)RSC_NOALLOC_MAX_BLOCKS * RSC_NOALLOC_MAX_GATES * 16)
-#define RSC_NA_RK_OFF (RSC_NA_PARTIALS_OFF + RSC_NA_PARTIALS_BYTES)
+ * The pulse kernel needs scratch memory beyond its inputs and outputs: an FP64
+ * accumulator per gate and lane, a completion counter, and the gate origins
+ * and weight tables in device memory.  rsc_make_pulse takes them from buffers
+ * rsc_worker_malloc allocated.  rsc_make_pulse_noalloc takes them from the
+ * fixed array below instead, so a caller that must not allocate device memory
+ * can still form a pulse from its own device buffers. */
+#define RSC_NA_ACC_OFF 0
+#define RSC_NA_ACC_BYTES ((size_t)RSC_NOALLOC_MAX_GATES * 4 * sizeof(double))
+#define RSC_NA_RK_OFF (RSC_NA_ACC_OFF + RSC_NA_ACC_BYTES)
 #define RSC_NA_RW_OFF (RSC_NA_RK_OFF + (size_t)RSC_NOALLOC_MAX_GATES * 4)
 #define RSC_NA_AW_OFF (RSC_NA_RW_OFF + (size_t)RSC_NOALLOC_MAX_RANGE_TABLE * 4)
 #define RSC_NA_COUNTER_OFF (RSC_NA_AW_OFF + (size_t)RSC_NOALLOC_MAX_ANGULAR_TABLE * 4)
@@ -833,7 +835,8 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_RK_OFF, rk, G * sizeof(float), cudaMemcpyHostToDevice, st));
     RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_RW_OFF, range_weight, range_n * sizeof(float), cudaMemcpyHostToDevice, st));
     RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_AW_OFF, angular_weight, angular_n * sizeof(float), cudaMemcpyHostToDevice, st));
-    /* the counter must start at zero; the partials are written before read */
+    /* the accumulator and the counter must start at zero */
+    RSC_CUDA(cudaMemsetAsync(b + RSC_NA_ACC_OFF, 0, (size_t)G * 4 * sizeof(double), st));
     RSC_CUDA(cudaMemsetAsync(b + RSC_NA_COUNTER_OFF, 0, sizeof(unsigned), st));
     /* launch geometry of the plain pulse kernel, capped to the scratch size */
     int dev = 0, sms = 0, per_sm = 1;
@@ -844,8 +847,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     RSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<0>, threads, smem));
     if (per_sm < 1) per_sm = 1;
     if (per_sm > 4) per_sm = 4;
-    int grid = sms * per_sm;
-    if (grid > RSC_NOALLOC_MAX_BLOCKS) grid = RSC_NOALLOC_MAX_BLOCKS;
+    const int grid = sms * per_sm;
     PulseArgs P;
     memset(&P, 0, sizeof(P));
     P.pos = reinterpret_cast<const float4 *>(pos4);
@@ -860,7 +862,10 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     memcpy(P.sim, sim_desc, sizeof(P.sim));
     P.rs = range_start;
     P.inv_delta = range_delta != 0.0f ? 1.0f / range_delta : 0.0f;
-    P.partials = b + RSC_NA_PARTIALS_OFF;
+    P.rdelta = range_delta;
+    P.rw_n = range_n;
+    for (uint32_t k = 0; k < 4; k++) P.rwv[k] = k < range_n ? range_weight[k] : 0.0f;
+    P.acc64 = reinterpret_cast<double *>(b + RSC_NA_ACC_OFF);
     P.counter = reinterpret_cast<unsigned *>(b + RSC_NA_COUNTER_OFF);
     P.pulse = reinterpret_cast<float4 *>(pulse4);
     /* sparse gate window when both edge weights are zero (see fill_pulse_args) */

@@ -272,10 +272,10 @@ __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned lon
     return t;
 }
 
-/* 6 blocks of 256 per SM (<= 42 registers): the step is a chain of dependent
+/* 5 blocks of 256 per SM (<= 51 registers): the step is a chain of dependent
  * loads (state, then 8 LES texels, then the debris tables), so resident warps
  * are what hides the latency */
-__global__ void __launch_bounds__(kAdvanceThreads, 6) k_advance(const AdvanceArgs a) {
+__global__ void __launch_bounds__(kAdvanceThreads, 5) k_advance(const AdvanceArgs a) {
     const unsigned b = blockIdx.x;
     if (b < a.rain_blocks) {
         unsigned long long j = (unsigned long long)b * kAdvanceThreads + threadIdx.x;
@@ -323,9 +323,12 @@ struct PulseArgs {
     unsigned G;
     float sim[16];
     float rs, inv_delta, win_lo, win_hi;
+    float rdelta;        /* gate spacing: the running sum's increment */
+    unsigned rw_n;       /* range weight table length; <= 4 is kept in rwv */
+    float rwv[4];
     int dense;
     int materialize;
-    void *partials;      /* gridDim.x * G * 4 accumulators (x2 for double-float) */
+    double *acc64;       /* G * 4 FP64 accumulators, zero between launches */
     unsigned *counter;
     float4 *pulse;
     double *pulse64;
@@ -339,6 +342,19 @@ __device__ __forceinline__ float range_weight(const PulseArgs &P, float d) {
     float dec0 = cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, P.rwd[2]), &f0);
     (void)cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 1.0f), 0.0f, P.rwd[2]), &f1);
     return cl_mix(__ldg(P.rw + (uint32_t)f0), __ldg(P.rw + (uint32_t)f1), dec0);
+}
+
+/* the same weight with a table of at most 4 entries held in the kernel
+ * parameters (the triangle of RS_set_range_weight_to_triangle has 3) */
+__device__ __forceinline__ float range_weight_reg(const PulseArgs &P, float d) {
+    if (P.rw_n > 4) return range_weight(P, d);
+    float f0, f1;
+    float dec0 = cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, P.rwd[2]), &f0);
+    (void)cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 1.0f), 0.0f, P.rwd[2]), &f1);
+    const uint32_t i0 = (uint32_t)f0, i1 = (uint32_t)f1;
+    const float w0 = i0 == 0 ? P.rwv[0] : (i0 == 1 ? P.rwv[1] : (i0 == 2 ? P.rwv[2] : P.rwv[3]));
+    const float w1 = i1 == 0 ? P.rwv[0] : (i1 == 1 ? P.rwv[1] : (i1 == 2 ? P.rwv[2] : P.rwv[3]));
+    return cl_mix(w0, w1, dec0);
 }
 
 /* the angular weight of scat_sig_aux (rs.cl:1066-1089) */

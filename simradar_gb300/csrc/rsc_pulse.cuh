@@ -4,9 +4,10 @@
  *
  * Each thread forms its scatterer's signal in registers and adds it only to the
  * gates the range weight can reach (the weights are the pass-1 weights, bit for
- * bit).  Sums go into per-warp gate bins in shared memory; each block writes one
- * partial per gate and the last block to finish adds the partials in block
- * order, so the pulse comes out of a single launch.
+ * bit).  Sums go into per-warp gate bins in shared memory; each block adds its
+ * sum per gate into an FP64 accumulator in global memory (one atomic per gate
+ * and lane) and the last block to finish converts it, so the pulse comes out
+ * of a single launch with no serial tail.
  *
  *   RSC_PULSE_PLAIN        FP32 throughout, as the reference; per-warp bins
  *                          updated with shared-memory atomics.
@@ -272,30 +273,29 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
                     bin_add<Acc>(wbins, 0xffffffffu, nz, gate, cw);
                 }
             } else {
-                /* weights first (gate origins from global memory: they do not
-                 * alias the shared-memory bins), then the atomic adds */
-                float w[kMaxCandidates];
-#pragma unroll
-                for (int j = 0; j < kMaxCandidates; j++) {
+                /* plain: one gate origin is loaded and advanced by the same
+                 * FP32 additions the reference's running sum makes
+                 * (rs.cl:1214), so every candidate's origin is bit-identical */
+                float rkj = 0.0f;
+                if (MODE == 0 && k_hi >= k_lo) rkj = __ldg(P.rk + k_lo);
+                for (int j = 0; j < maxc; j++) {
                     const int gate = k_lo + j;
-                    w[j] = 0.0f;
-                    if (j < maxc && gate <= k_hi) {
+                    if (gate <= k_hi) {
+                        float w;
                         if constexpr (MODE == 1) {
-                            w[j] = weight_comp(P.rw, P.rwd, r - __ldg(P.rk + gate), r_lo - __ldg(P.rk_lo + gate));
+                            w = weight_comp(P.rw, P.rwd, r - __ldg(P.rk + gate), r_lo - __ldg(P.rk_lo + gate));
                         } else {
-                            w[j] = range_weight(P, r - __ldg(P.rk + gate));
+                            w = range_weight_reg(P, r - rkj);
+                        }
+                        if (w != 0.0f) {
+                            float *b = fbins + (size_t)gate * kBinStride32;
+                            atomicAdd(b + 0, w * c.v[0]);
+                            atomicAdd(b + 1, w * c.v[1]);
+                            atomicAdd(b + 2, w * c.v[2]);
+                            atomicAdd(b + 3, w * c.v[3]);
                         }
                     }
-                }
-#pragma unroll
-                for (int j = 0; j < kMaxCandidates; j++) {
-                    if (w[j] != 0.0f) {
-                        float *b = fbins + (size_t)(k_lo + j) * kBinStride32;
-                        atomicAdd(b + 0, w[j] * c.v[0]);
-                        atomicAdd(b + 1, w[j] * c.v[1]);
-                        atomicAdd(b + 2, w[j] * c.v[2]);
-                        atomicAdd(b + 3, w[j] * c.v[3]);
-                    }
+                    rkj = rkj + P.rdelta;
                 }
             }
             /* a non-finite signal meets every gate (0 * inf = NaN in pass 1) */
@@ -360,11 +360,14 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     }
     __syncthreads();
 
-    /* block partial: warp bins summed in warp order */
+    /* block sum of each output (warp bins in warp order), added into the
+     * grid's FP64 accumulator with one global atomic per output: no block
+     * waits on another, and FP64 carries the FP32 and double-float block sums
+     * exactly enough that the order of the atomics does not show */
     const unsigned outs = G * 4;
-    bin_t *part = reinterpret_cast<bin_t *>(P.partials) + (size_t)blockIdx.x * outs * Acc::kWords;
     for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
         const unsigned k = o >> 2, l = o & 3u;
+        double v;
         if constexpr (Acc::kWords == 2) {
             float hi = 0.0f, lo = 0.0f;
             for (unsigned wv = 0; wv < nwarps; wv++) {
@@ -374,13 +377,13 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
                 hi = s;
                 lo = lo + (e + b[4 + l]);
             }
-            reinterpret_cast<float *>(part)[o] = hi;
-            reinterpret_cast<float *>(part)[outs + o] = lo;
+            v = (double)hi + (double)lo;
         } else {
             bin_t acc = (bin_t)0;
             for (unsigned wv = 0; wv < nwarps; wv++) acc = acc + bins[(size_t)wv * words + k * kMain + l];
-            part[o] = acc;
+            v = (double)acc;
         }
+        if (v != 0.0) atomicAdd(P.acc64 + o, v);
     }
     __threadfence();
     __syncthreads();
@@ -392,42 +395,14 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    /* last block: sum the block partials in block order; warp w takes
-     * outputs w, w + nwarps, ...; lanes stride over blocks, then a fixed
-     * shuffle tree */
-    const unsigned nb = gridDim.x;
-    for (unsigned o = warp; o < outs; o += nwarps) {
-        if constexpr (Acc::kWords == 2) {
-            const float *pf = reinterpret_cast<const float *>(P.partials);
-            float hi = 0.0f, lo = 0.0f;
-            for (unsigned b = lane; b < nb; b += 32) {
-                const float *pb = pf + (size_t)b * outs * 2;
-                float s, e;
-                two_sum(hi, __ldcg(pb + o), s, e);
-                hi = s;
-                lo = lo + (e + __ldcg(pb + outs + o));
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                float ohi = __shfl_down_sync(0xffffffffu, hi, off);
-                float olo = __shfl_down_sync(0xffffffffu, lo, off);
-                float s, e;
-                two_sum(hi, ohi, s, e);
-                hi = s;
-                lo = lo + (e + olo);
-            }
-            if (lane == 0) reinterpret_cast<float *>(P.pulse)[o] = hi + lo;
-        } else {
-            const bin_t *pf = reinterpret_cast<const bin_t *>(P.partials);
-            bin_t acc = (bin_t)0;
-            for (unsigned b = lane; b < nb; b += 32) acc = acc + __ldcg(pf + (size_t)b * outs + o);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, off);
-            if (lane == 0) {
-                reinterpret_cast<float *>(P.pulse)[o] = (float)acc;
-                if (MODE == 2) P.pulse64[o] = (double)acc;
-            }
-        }
+    /* last block: every other block's atomics are visible (each fenced
+     * before taking its ticket); convert, and leave the accumulator and the
+     * counter at zero for the next launch */
+    for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
+        const double v = __ldcg(P.acc64 + o);
+        reinterpret_cast<float *>(P.pulse)[o] = (float)v;
+        if (MODE == 2) P.pulse64[o] = v;
+        P.acc64[o] = 0.0;
     }
     if (threadIdx.x == 0) *P.counter = 0u;
 }

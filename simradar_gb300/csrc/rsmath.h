@@ -17,13 +17,14 @@
  *   - sin/cos: Cody-Waite reduction by pi/2 split in three floats, applied
  *     with fmaf (the first step is exact for |x| < 2^22 * pi/2), then the
  *     Taylor polynomials of sin (to x^9) and cos (to x^10) on [-pi/4, pi/4].
- *   - log: x = m 2^e with m in [sqrt(1/2), sqrt(2)), log(m) = 2 atanh(s),
- *     s = (m-1)/(m+1), series to s^9; e*ln2 added as a 16-bit head + tail.
- *   - log1p: Goldberg's identity log1p(x) = log(u) * x / (u - 1), u = 1 + x
- *     (D. Goldberg, "What every computer scientist should know about
- *     floating-point arithmetic", ACM Computing Surveys 23(1), 1991, thm. 4)
- *     outside sqrt(1/2) - 1 < x < sqrt(2) - 1, the atanh series on
- *     s = x / (2 + x) inside.
+ *   - log: x = m 2^e with m in [sqrt(1/2), sqrt(2)), log(m) = f - f^2/2 +
+ *     f^3 P(f), f = m - 1, P a degree-7 least-squares fit made for this file
+ *     (relative error 7.7e-9); e*ln2 added as a 16-bit head + tail.  No
+ *     division.
+ *   - log1p: the same polynomial on x inside sqrt(1/2) - 1 < x < sqrt(2) - 1;
+ *     outside, log(u) + e / u with u = 1 + x rounded and e = (1 + x) - u
+ *     formed exactly (the correction is below an ulp, so 1/u comes from the
+ *     exponent and one Newton step, again without a division).
  *   - asin/acos: Taylor series of asin to s^21 on |s| <= 1/2 and the
  *     half-angle identity acos(x) = 2 asin(sqrt((1-x)/2)) above.
  *   - atan/atan2: reduction to [0, 1], then to |u| <= tan(pi/8) by
@@ -162,15 +163,21 @@ RSM_FN float rsm_cosf(float x) {
     return c;
 }
 
-/* log((1 + s) / (1 - s)) = 2 atanh(s) = 2 s + s z (2/3 + z (2/5 + z (2/7 + z 2/9))),
- * z = s^2, for |s| <= 3 - 2 sqrt(2) */
-RSM_FN float rsm_log_core(float s) {
-    float z = s * s;
-    float p = 0x1.c71c72p-3f;                 /* 2/9 */
-    p = fmaf(p, z, 0x1.24924ap-2f);           /* 2/7 */
-    p = fmaf(p, z, 0x1.99999ap-2f);           /* 2/5 */
-    p = fmaf(p, z, 0x1.555556p-1f);           /* 2/3 */
-    return fmaf(s * z, p, 2.0f * s);
+/* log(1 + f) for f in [sqrt(1/2) - 1, sqrt(2) - 1]: f - f^2 / 2 + f^3 P(f)
+ * with P of degree 7, a weighted least-squares fit of the relative error
+ * (7.7e-9 with these single-precision coefficients); no division. */
+RSM_FN float rsm_log1p_core(float f) {
+    float p = -0x1.38b4a6p-4f;
+    p = fmaf(p, f, 0x1.055b42p-3f);
+    p = fmaf(p, f, -0x1.0d8558p-3f);
+    p = fmaf(p, f, 0x1.22da24p-3f);
+    p = fmaf(p, f, -0x1.547242p-3f);
+    p = fmaf(p, f, 0x1.99a008p-3f);
+    p = fmaf(p, f, -0x1.000228p-2f);
+    p = fmaf(p, f, 0x1.555554p-2f);
+    float z = f * f;
+    float t = fmaf(f * z, p, -0.5f * z);
+    return f + t;
 }
 
 /* natural logarithm */
@@ -197,7 +204,7 @@ RSM_FN float rsm_logf(float x) {
         e += 1;
     }
     float f = m - 1.0f;                       /* exact (Sterbenz) */
-    float lm = rsm_log_core(f / (2.0f + f));
+    float lm = rsm_log1p_core(f);
     float fe = (float)e;
     return fe * RSM_LN2_HI + fmaf(fe, RSM_LN2_LO, lm);
 }
@@ -208,18 +215,25 @@ RSM_FN float rsm_log1pf(float x) {
         return x;
     }
     if (x > -0x1.2bec34p-2f && x < 0x1.a8279ap-2f) {
-        /* 1 + x in [sqrt(1/2), sqrt(2)): the series on s = x / (2 + x)
-         * directly, without rounding 1 + x */
-        return rsm_log_core(x / (2.0f + x));
+        /* 1 + x in [sqrt(1/2), sqrt(2)): the polynomial on x directly,
+         * without rounding 1 + x */
+        return rsm_log1p_core(x);
     }
     float u = 1.0f + x;
-    if (u == 1.0f) {
-        return x;
+    if (u == INFINITY || !(u > 0.0f)) {
+        return rsm_logf(u);
     }
-    if (u == INFINITY) {
-        return rsm_logf(x);
-    }
-    return rsm_logf(u) * (x / (u - 1.0f));
+    /* log(1 + x) = log(u) + log(1 + e / u), e = (1 + x) - u exactly (u - 1 is
+     * exact here); e / u < 2^-24, so log(1 + e / u) = e / u to far below an
+     * ulp and 1 / u needs only a few correct bits: 2^-k (1.5 - m / 2) for
+     * u = m 2^k, m in [1, 2), refined once by Newton's step. */
+    float e = x - (u - 1.0f);
+    uint32_t b = rsm_f2u(u);
+    float m = rsm_u2f((b & 0x007fffffu) | 0x3f800000u);
+    float y = 1.5f - 0.5f * m;
+    y = y * (2.0f - m * y);
+    float inv = y * rsm_u2f((uint32_t)(254 - (int)((b >> 23) & 0xff)) << 23);
+    return rsm_logf(u) + e * inv;
 }
 
 /* asin on |s| <= 1/2 : s + s z P(z), z = s^2 (Taylor series to s^21) */
