@@ -17,9 +17,25 @@ simradar_gb300/synth.py).
   --impl reference  times the CPU restatement of the reference algorithm
          (the oracle: O(N G) pass 1 + 2-pass reduction, OpenMP on every host
          core) on the same workload.
+
+Extra sections on one GPU (added to the same JSON line):
+  precision  8,388,608 scatterers with the box and gates 30 km out: plain and
+             compensated pulses against the FP64 pulse of the same state
+             (per-gate relative I/Q error, Zdr / rhohv bias over the pulse
+             series) and the throughput of each form.
+  batch      64 instances (scatterers log-uniform 65,536-4,194,304, debris
+             0-4096 per type, N0 4000-16000, PPI / RHI mix) in the
+             compensated form: batched (two launches per step for all, CUDA
+             graph, autotuned pulse shape) against the same instances run back
+             to back one after another.
+  large      33,554,432 rain + 131,072 debris, LES 352x352x160, RHI
+             0.5-20 deg at 0.02 deg, compensated form, I/Q streamed to pinned
+             host buffers every 100 pulses, one LES slot refilled on the copy
+             stream during the run.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -37,6 +53,7 @@ DEBRIS = ((1, 1024), (3, 1024), (6, 1024))
 GATES = 40
 METRIC = "pulses/s and scatterer-updates/s at 2M scatterers; HBM roofline frac; I/Q err vs FP64"
 UNIT = "pulses/s"
+SECTIONS = ("precision", "batch", "large")
 
 
 def workload_config(n_rain):
@@ -144,6 +161,17 @@ def build_scene(n_rain):
     return S
 
 
+def traffic_bytes(n_rain, n_deb, gates):
+    """Algorithmic HBM bytes per launch.  Advance: a rain scatterer reads pos
+    and vel and writes pos, vel and rcs (32 + 48 B); a debris scatterer reads
+    pos, ori, vel, tum and writes those and rcs (64 + 80 B); respawn seeds
+    and the LES / table texels (reused across scatterers) are not counted.
+    Pulse: pos and rcs read once (32 B) and the gates written."""
+    adv = 80 * n_rain + 144 * n_deb
+    pul = 32 * (n_rain + n_deb) + 16 * gates
+    return adv, pul
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -166,12 +194,287 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def run_ours(args, rank, world):
-    import ctypes
+def timed_steps(torch, W, pop, sd_seq, steps, flush=None, les_id=0):
+    """Per-step (pulse ms, advance ms) with CUDA events on the worker's
+    stream; `flush` (a device tensor larger than L2) is rewritten between
+    steps, outside the events."""
+    stream = torch.cuda.ExternalStream(W.stream)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+        ev[k][0].record(stream)
+        W.make_pulse(sd_seq[k % len(sd_seq)])
+        ev[k][1].record(stream)
+        W.advance_time(pop, les_id, sd_seq[k % len(sd_seq)])
+        ev[k][2].record(stream)
+    W.synchronize()
+    torch.cuda.synchronize()
+    t_pulse = [ev[k][0].elapsed_time(ev[k][1]) for k in range(steps)]
+    t_adv = [ev[k][1].elapsed_time(ev[k][2]) for k in range(steps)]
+    return t_pulse, t_adv
 
-    from simradar_gb300 import build as B
+
+# ------------------------------------------------------------------ precision
+def gate_stats(series):
+    """Zdr (dB) and rhohv per gate from a (pulses, gates, 4) I/Q series."""
+    s = series.astype(np.float64)
+    h = s[..., 0] + 1j * s[..., 1]
+    v = s[..., 2] + 1j * s[..., 3]
+    ph = (np.abs(h) ** 2).sum(axis=0)
+    pv = (np.abs(v) ** 2).sum(axis=0)
+    ok = (ph > 0) & (pv > 0)
+    zdr = np.where(ok, 10.0 * np.log10(np.where(ok, ph, 1.0) / np.where(ok, pv, 1.0)), 0.0)
+    rho = np.where(ok, np.abs((h * np.conj(v)).sum(axis=0)) / np.sqrt(np.where(ok, ph * pv, 1.0)), 0.0)
+    return zdr, rho, ok
+
+
+def iq_errors(got, ref):
+    """Per-gate complex relative error |got - ref| / |ref| for H and V."""
+    g = got.astype(np.float64)
+    r = ref.astype(np.float64)
+    e_h = np.hypot(g[..., 0] - r[..., 0], g[..., 1] - r[..., 1])
+    e_v = np.hypot(g[..., 2] - r[..., 2], g[..., 3] - r[..., 3])
+    m_h = np.hypot(r[..., 0], r[..., 1])
+    m_v = np.hypot(r[..., 2], r[..., 3])
+    e = np.concatenate([e_h.ravel(), e_v.ravel()])
+    m = np.concatenate([m_h.ravel(), m_v.ravel()])
+    nz = m > 0
+    rel = e[nz] / m[nz]
+    return {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt((rel ** 2).mean())),
+            "p99_rel": float(np.percentile(rel, 99)), "values": int(rel.size)}
+
+
+def bench_precision(torch, rsc, synth, dev, steps):
+    n = 8388608
+    S = synth.make_scene(num_rain=n, gates=GATES, les_count=1, range_offset=30000.0, seed=4242,
+                         scan=synth.ppi_positions(0.7, -0.6, 0.6, 0.012))
+    sd_seq = [synth.pulse_sim_desc(S, k, tic=k * 1e-3) for k in range(len(S.scan))]
+    pop = synth.population(S)
+    W = rsc.Worker(dev)
+    synth.load_worker(W, S)
+    S.state = None
+    n_err = 64
+    got = {m: np.zeros((n_err, GATES, 4), np.float32) for m in (0, 1, 2)}
+    for k in range(n_err):
+        sd = sd_seq[k % len(sd_seq)]
+        for m in (2, 1, 0):
+            W.set_precision(m)
+            W.make_pulse(sd)
+            W.download_pulse(1.0, out=got[m][k])
+        W.advance_time(pop, 0, sd)
+    z64, r64, ok = gate_stats(got[2])
+    out = {"workload": "8,388,608 rain, box and 40 gates 30 km out (gates from 31,850 m), PPI 0.7 deg "
+                       "-0.6..0.6 deg / 0.012 deg, concept DBU; errors over %d pulses against the FP64 pulse "
+                       "(RSC_PULSE_F64) of the same state" % n_err}
+    for m, name in ((1, "compensated"), (0, "plain")):
+        z, r, _ = gate_stats(got[m])
+        e = iq_errors(got[m], got[2])
+        e["zdr_bias_db_max"] = float(np.abs(z - z64)[ok].max()) if ok.any() else None
+        e["rhohv_bias_max"] = float(np.abs(r - r64)[ok].max()) if ok.any() else None
+        out[name] = e
+    timing = {}
+    for m, name in ((0, "plain"), (1, "compensated")):
+        W.set_precision(m)
+        for k in range(3):
+            W.make_pulse(sd_seq[k])
+            W.advance_time(pop, 0, sd_seq[k])
+        tp, ta = timed_steps(torch, W, pop, sd_seq, steps)
+        timing[name] = {"pulses_per_s": steps / ((sum(tp) + sum(ta)) / 1000.0),
+                        "pulse_ms": statistics.mean(tp), "advance_ms": statistics.mean(ta)}
+    out["throughput"] = timing
+    out["timed_steps"] = steps
+    W.close()
+    return out
+
+
+# ---------------------------------------------------------------------- batch
+def batch_scenes(synth, count, seed=2024):
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(65536), math.log(4194304), count)).astype(np.int64)
+    deb = rng.integers(0, 4097, size=(count, 3))
+    n0 = rng.uniform(4000.0, 16000.0, count)
+    base = synth.make_scene(num_rain=1, les_count=1, with_tables=True)
+    scenes = []
+    for i in range(count):
+        if i % 2 == 0:
+            scan = synth.ppi_positions(float(rng.uniform(1.0, 6.0)), -12.0, 12.0, 0.24)
+        else:
+            scan = synth.rhi_positions(float(rng.uniform(-6.0, 6.0)), 0.5, 20.0, 0.2)
+        debris = [(o, int(c)) for o, c in zip((synth.OBJ_LEAF, synth.OBJ_WOODBOARD_2X4, synth.OBJ_BRICK), deb[i])
+                  if c > 0]
+        S = synth.make_scene(num_rain=int(sizes[i]), debris=debris, gates=GATES, les_count=1, with_tables=False,
+                             seed=1000 + i, scan=scan, dsd_n0=float(n0[i]))
+        S.les, S.les_cfg, S.les_desc = base.les, base.les_cfg, base.les_desc
+        scenes.append(S)
+    return scenes
+
+
+def bench_batch(torch, rsc, synth, dev, steps):
+    count = 64
+    scenes = batch_scenes(synth, count)
+    ws = []
+    for S in scenes:
+        W = rsc.Worker(dev)
+        synth.load_worker(W, S)
+        W.set_precision(rsc.PULSE_COMPENSATED)
+        S.state = None
+        ws.append(W)
+    pops = [synth.population(S) for S in scenes]
+    total = sum(S.num_scats for S in scenes)
+
+    def sims(k0, K):
+        a = np.zeros((K, count, 16), np.float32)
+        for j in range(K):
+            for i, S in enumerate(scenes):
+                a[j, i] = synth.pulse_sim_desc(S, k0 + j, tic=(k0 + j) * 1e-3)
+        return a
+
+    B = rsc.Batch(ws)
+    B.set_populations(pops)
+    B.set_precision(rsc.PULSE_COMPENSATED)
+    shape = B.autotune(sims(0, 1)[0])
+    les = np.zeros((steps, count), np.int32)
+    out = np.empty((steps, count, B.max_gates, 4), np.float32)
+    bstream = torch.cuda.ExternalStream(B.stream)
+    res = {}
+    for use_graph in (True, False):
+        B.run(sims(0, steps), les, out=out, use_graph=use_graph)       # warm-up (and graph capture)
+        sd = sims(steps, steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        B.synchronize()
+        l0 = B.launch_count
+        t0 = time.perf_counter()
+        e0.record(bstream)
+        B.run(sd, les, out=out, use_graph=use_graph)
+        e1.record(bstream)
+        wall = time.perf_counter() - t0
+        e1.synchronize()
+        dev_ms = e0.elapsed_time(e1)
+        key = "batched_graph" if use_graph else "batched_stream"
+        res[key] = {"pulses_per_s": count * steps / wall, "device_pulses_per_s": count * steps / (dev_ms / 1e3),
+                    "launches": B.launch_count - l0}
+    B.close()
+    # back to back: each instance runs its steps alone, one after another
+    hp = torch.empty((GATES, 4), dtype=torch.float32).pin_memory().numpy()
+    for W, S, p in zip(ws, scenes, pops):
+        for k in range(2):
+            sd = synth.pulse_sim_desc(S, k)
+            W.make_pulse(sd)
+            W.advance_time(p, 0, sd)
+    torch.cuda.synchronize()
+    seqs = [[synth.pulse_sim_desc(S, k, tic=k * 1e-3) for k in range(steps)] for S in scenes]
+    t0 = time.perf_counter()
+    for W, seq, p in zip(ws, seqs, pops):
+        for k in range(steps):
+            W.make_pulse(seq[k])
+            W.download_pulse(1.0, out=hp)
+            W.advance_time(p, 0, seq[k])
+        W.synchronize()
+    wall_b2b = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for W, seq, p in zip(ws, seqs, pops):
+        for k in range(steps):
+            W.make_pulse(seq[k])
+            W.advance_time(p, 0, seq[k])
+        W.synchronize()
+    wall_b2b_nodl = time.perf_counter() - t0
+    for W in ws:
+        W.close()
+    res["back_to_back"] = {"pulses_per_s": count * steps / wall_b2b,
+                           "pulses_per_s_no_download": count * steps / wall_b2b_nodl}
+    res["speedup_vs_back_to_back"] = res["batched_graph"]["pulses_per_s"] / res["back_to_back"]["pulses_per_s"]
+    res["workload"] = ("64 instances, scatterers log-uniform 65,536-4,194,304 (total %d), debris 0-4096 per type, "
+                       "Marshall-Palmer N0 4000-16000, PPI / RHI alternating, %d gates, compensated form; %d steps "
+                       "timed per instance, pulses copied to the host (batched: once per run; back to back: per "
+                       "pulse)" % (total, GATES, steps))
+    res["pulse_shape"] = {"warps": shape[0], "blocks_per_sm": shape[1]}
+    res["scatterer_updates_per_s"] = res["batched_graph"]["pulses_per_s"] / count * total
+    return res
+
+
+# ---------------------------------------------------------------------- large
+def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
+    n_rain = 33554432
+    cfg = synth.LESConfig(nx=352, ny=352, nz=160)
+    debris = [(synth.OBJ_LEAF, 43691), (synth.OBJ_WOODBOARD_2X4, 43691), (synth.OBJ_BRICK, 43690)]
+    S = synth.make_scene(num_rain=n_rain, debris=debris, gates=GATES, les_cfg=cfg, les_count=2, seed=777,
+                         scan=synth.rhi_positions(0.0, 0.5, 20.0, 0.02))
+    pop = synth.population(S)
+    W = rsc.Worker(dev)
+    synth.load_worker(W, S, les_slot_volumes=(0,))
+    W.set_precision(rsc.PULSE_COMPENSATED)
+    nscat = S.num_scats
+    S.state = None
+    # the next LES frame in page-locked memory, for the refill of slot 1
+    nxt = S.les[1]
+    pin_u = torch.from_numpy(np.ascontiguousarray(nxt.uvwt)).pin_memory()
+    pin_c = torch.from_numpy(np.ascontiguousarray(nxt.cpxx)).pin_memory()
+    B = rsc.Batch([W])
+    B.set_populations([pop])
+    B.set_precision(rsc.PULSE_COMPENSATED)
+    ring = [torch.empty((chunk, 1, B.max_gates, 4), dtype=torch.float32).pin_memory() for _ in range(2)]
+    stream = torch.cuda.ExternalStream(B.stream)
+    iq = np.zeros((chunks * chunk, GATES, 4), np.float32)
+
+    def sims(k0):
+        a = np.zeros((chunk, 1, 16), np.float32)
+        for j in range(chunk):
+            a[j, 0] = synth.pulse_sim_desc(S, k0 + j, tic=(k0 + j) * 1e-3)
+        return a
+
+    def les_ids(slot):
+        return np.full((chunk, 1), slot, np.int32)
+
+    B.autotune(sims(0)[0])
+    B.run(sims(0), les_ids(0), out=ring[0].numpy())     # warm-up and graph capture
+    B.synchronize()
+    done = [None, None]
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    swap_at = chunks // 2
+    for c in range(chunks):
+        r = c % 2
+        if done[r] is not None:
+            done[r][0].synchronize()
+            iq[done[r][1] * chunk:(done[r][1] + 1) * chunk] = ring[r].numpy()[:, 0, :GATES]
+        slot = 1 if c >= swap_at else 0
+        B.run(sims(chunk * (c + 1)), les_ids(slot), out=ring[r].numpy(), wait=False)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        done[r] = (ev, c)
+        if c == swap_at - 1:
+            # refill slot 1 while this chunk runs on slot 0
+            B.set_les_async(0, 1, pin_u.numpy(), pin_c.numpy())
+    e1.record(stream)
+    for r in range(2):
+        if done[r] is not None:
+            done[r][0].synchronize()
+            iq[done[r][1] * chunk:(done[r][1] + 1) * chunk] = ring[r].numpy()[:, 0, :GATES]
+    B.synchronize()
+    wall = time.perf_counter() - t0
+    dev_ms = e0.elapsed_time(e1)
+    pulses = chunks * chunk
+    B.close()
+    W.close()
+    return {"workload": "33,554,432 rain + 131,072 debris (leaf / 2x4 board / brick), LES 352x352x160, RHI 0.5-20 "
+                        "deg / 0.02 deg, %d gates, compensated form; %d pulses in chunks of %d streamed to pinned "
+                        "host buffers, LES slot 1 refilled (2 x %d MB) on the copy stream during chunk %d"
+                        % (GATES, pulses, chunk, int(nxt.uvwt.nbytes / 1e6), swap_at - 1),
+            "pulses_per_s": pulses / wall, "device_pulses_per_s": pulses / (dev_ms / 1e3),
+            "scatterer_updates_per_s": pulses / wall * nscat, "pulses": pulses,
+            "iq_finite": bool(np.isfinite(iq).all()), "iq_nonzero_pulses": int((np.abs(iq).sum(axis=(1, 2)) > 0).sum())}
+
+
+def run_ours(args, rank, world):
+    from simradar_gb300 import build as Bld
     from simradar_gb300 import rsc, synth
-    B.build()
+    Bld.build()
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -187,40 +490,22 @@ def run_ours(args, rank, world):
     hp = host_pulse.numpy()
     gain = float(S.gain)
 
-    def step(k):
-        sd = sd_seq[k % len(sd_seq)]
-        W.make_pulse(sd)
-        W.advance_time(pop, 0, sd)
-
     # warm-up
     for k in range(args.warmup):
-        step(k)
+        W.make_pulse(sd_seq[k % len(sd_seq)])
+        W.advance_time(pop, 0, sd_seq[k % len(sd_seq)])
     W.synchronize()
 
     # device-timed value: per-step events, L2 flushed between steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = W.launch_count
     clocks = ClockSampler(dev)
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(k))
-            ev[k][0].record(stream)
-        W.make_pulse(sd_seq[k % len(sd_seq)])
-        ev[k][1].record(stream)
-        W.advance_time(pop, 0, sd_seq[k % len(sd_seq)])
-        ev[k][2].record(stream)
-    W.synchronize()
-    torch.cuda.synchronize()
+    t_pulse, t_adv = timed_steps(torch, W, pop, sd_seq, args.steps, flush=flush)
     if world > 1:
         torch.distributed.barrier()
     launches = W.launch_count - launches0
-    t_pulse = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
-    t_adv = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
     total_ms = sum(t_pulse) + sum(t_adv)
 
     # e2e through the C ABI with host buffers
@@ -247,27 +532,51 @@ def run_ours(args, rank, world):
     e2e = world * args.steps / (e2e_ms / 1000.0)
     peak, peak_kind = load_peaks()
     n_deb = sum(c for _, c in DEBRIS)
-    adv_bytes = 64 * N_RAIN + 128 * n_deb
-    pulse_bytes = 32 * (N_RAIN + n_deb) + 16 * G
+    adv_bytes, pulse_bytes = traffic_bytes(N_RAIN, n_deb, G)
     adv_ms = statistics.mean(t_adv)
     pul_ms = statistics.mean(t_pulse)
     adv_gbs = adv_bytes / (adv_ms * 1e-3) / 1e9
     pul_gbs = pulse_bytes / (pul_ms * 1e-3) / 1e9
     if adv_ms >= pul_ms:
         dom = {"kernel": "k_advance", "achieved": adv_gbs, "traffic": load_traffic("k_advance_traffic")}
-        other = {"kernel": "k_pulse<0>", "achieved": pul_gbs, "ms": pul_ms, "bytes_per_launch": pulse_bytes}
+        other = {"kernel": "k_pulse<0>", "achieved": pul_gbs, "ms": pul_ms, "bytes_per_launch": pulse_bytes,
+                 "frac": pul_gbs / peak}
         dom_bytes = adv_bytes
     else:
         dom = {"kernel": "k_pulse<0>", "achieved": pul_gbs, "traffic": load_traffic("k_pulse_traffic")}
-        other = {"kernel": "k_advance", "achieved": adv_gbs, "ms": adv_ms, "bytes_per_launch": adv_bytes}
+        other = {"kernel": "k_advance", "achieved": adv_gbs, "ms": adv_ms, "bytes_per_launch": adv_bytes,
+                 "frac": adv_gbs / peak}
         dom_bytes = pulse_bytes
     roofline = {"bound": "hbm", "achieved": dom["achieved"], "peak": peak, "unit": "GB/s",
                 "frac": dom["achieved"] / peak, "traffic": dom["traffic"], "kernel": dom["kernel"],
                 "algorithmic_bytes_per_launch": dom_bytes, "peak_kind": peak_kind, "other_kernel": other}
+
+    # the compensated form on the same workload
+    W.set_precision(rsc.PULSE_COMPENSATED)
+    csteps = min(args.steps, 100)
+    for k in range(3):
+        W.make_pulse(sd_seq[k])
+        W.advance_time(pop, 0, sd_seq[k])
+    ct_p, ct_a = timed_steps(torch, W, pop, sd_seq, csteps, flush=flush)
+    comp = {"pulses_per_s": csteps / ((sum(ct_p) + sum(ct_a)) / 1000.0), "pulse_ms": statistics.mean(ct_p),
+            "advance_ms": statistics.mean(ct_a), "steps": csteps}
+    W.close()
+    del flush
+    torch.cuda.empty_cache()
+
+    extras = {}
+    if world == 1:
+        wanted = [s for s in args.sections.split(",") if s in SECTIONS]
+        if "precision" in wanted:
+            extras["precision"] = bench_precision(torch, rsc, synth, dev, steps=min(args.steps, 50))
+        if "batch" in wanted:
+            extras["batch"] = bench_batch(torch, rsc, synth, dev, steps=40)
+        if "large" in wanted:
+            extras["large"] = bench_large(torch, rsc, synth, dev, chunks=4)
+
     # CPU baseline: the oracle on a bounded sample of the same workload
     cpu = None
     if not args.no_cpu_baseline:
-        W.close()
         cpu_value, cores = cpu_reference(S, pulses=12, warm=1)
         cpu = {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "12 full-size pulses (make_pulse + advance_time) after 1 warm, OpenMP on all host cores"}
@@ -284,10 +593,10 @@ def run_ours(args, rank, world):
         "gpu_launches": int(launches),
         "scatterer_updates_per_s": value * S.num_scats,
         "kernel_ms": {"k_pulse<0>": pul_ms, "k_advance": adv_ms},
+        "compensated": comp,
     }
+    line.update(extras)
     print(json.dumps(line))
-    if args.no_cpu_baseline:
-        W.close()
 
 
 def main():
@@ -297,6 +606,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sections", default=",".join(SECTIONS),
+                    help="extra one-GPU sections to run (comma list of %s; '' for none)" % ", ".join(SECTIONS))
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -171,6 +171,77 @@ int rsc_launch_count(rsc_worker *w, uint64_t *count);
  * time with events on it). */
 int rsc_get_stream(rsc_worker *w, void **stream);
 
+/* ---- launch-shape autotuning (additive) ----
+ * Time the pulse kernel of this worker at each candidate shape (warps per
+ * block 4 / 8 / 16 and 1-4 resident blocks per SM) on the current state and
+ * keep the fastest for later rsc_make_pulse calls.  sim_desc is the beam to
+ * time with; the state is not changed (the pulse is recomputed). */
+int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *blocks_per_sm_out);
+
+/* ---- batching form (additive; no counterpart in rs.c) ----
+ * A batch runs many emulation instances -- each an rsc_worker with its own
+ * state, tables, gates, concept and population, all on one device -- one
+ * time step at a time, with two launches per step for all of them (pulse,
+ * then advance, the order of simradar's loop, simradar.c:1032-1070).  Each
+ * instance evolves exactly as it would alone. */
+typedef struct rsc_batch rsc_batch;
+
+/* The workers must be allocated and have their tables set.  The batch keeps
+ * the pointers; free it before the workers. */
+int rsc_batch_create(rsc_worker *const *workers, int count, rsc_batch **out);
+int rsc_batch_free(rsc_batch *b);
+
+/* Population layout of every instance (count entries). */
+int rsc_batch_set_populations(rsc_batch *b, const rsc_population *pops);
+
+/* RSC_PULSE_PLAIN / COMPENSATED / F64 for every instance. */
+int rsc_batch_set_precision(rsc_batch *b, int mode);
+
+/* Choose the batched pulse kernel's shape (warps per block 4 / 8 / 16 and
+ * 1-4 resident blocks per SM) by timing it on the current state with the
+ * given per-instance sim_descs (count x 16 floats, LES slot 0).  The state is
+ * not changed. */
+int rsc_batch_autotune(rsc_batch *b, const float *sim_descs);
+
+/* Run `steps` time steps of every instance: for step k and instance i the
+ * pulse for sim_descs[(k * count + i) * 16 ...] is formed, then the instance
+ * advances with LES slot les_ids[k * count + i].  The pulses (range_count
+ * float4 per instance, no gain applied) are copied to pulses_out as
+ * [k][i][max_gates] float4 if it is not NULL.  With use_graph the 2 * steps
+ * launches are captured once in a CUDA graph (per step count) and replayed.
+ * Returns after the pulses are on the host (or the work is queued when
+ * pulses_out is NULL; rsc_batch_synchronize waits). */
+int rsc_batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids, float *pulses_out,
+                  int use_graph);
+/* As rsc_batch_run, but returns once the work and the copy of the pulses are
+ * queued: pulses_out must stay valid until rsc_batch_synchronize (page-locked
+ * memory keeps the copy asynchronous; the I/Q streaming of long runs issues
+ * one such call per block of pulses into a ring of pinned buffers).  The
+ * descriptors are taken before the call returns. */
+int rsc_batch_run_async(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids, float *pulses_out,
+                        int use_graph);
+int rsc_batch_synchronize(rsc_batch *b);
+
+/* Refill LES slot `slot` of instance `index` (a slot already set with
+ * rsc_set_les, same dimensions and descriptor) on the batch's copy stream:
+ * the copy starts once the runs that read the slot are done and overlaps the
+ * runs queued meanwhile on the other slot; the first later run that reads
+ * the slot waits for it.  The host buffers (page-locked for the copy to be
+ * asynchronous) must stay valid until rsc_batch_synchronize.  Replaces the
+ * blocking frame swap of RS_set_vel_data inside RS_advance_time
+ * (rs.c:2854-2978, rs.c:5188-5200) for batched runs. */
+int rsc_batch_set_les_async(rsc_batch *b, int index, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx,
+                            uint32_t ny, uint32_t nz);
+/* The largest gate count of the batch (the row length of pulses_out). */
+int rsc_batch_max_gates(rsc_batch *b, int *max_gates);
+/* Kernel launches the batch has issued (2 per step with scatterers to
+ * advance, plus the autotuner's). */
+int rsc_batch_launch_count(rsc_batch *b, uint64_t *count);
+/* The CUDA stream the batch issues on. */
+int rsc_batch_get_stream(rsc_batch *b, void **stream);
+/* The pulse shape chosen by rsc_batch_autotune (0, 0 before it runs). */
+int rsc_batch_get_shape(rsc_batch *b, int *warps, int *blocks_per_sm);
+
 /* Limits of rsc_make_pulse_noalloc (its scratch is a fixed device array of
  * about 9 KB per GPU that loads this library). */
 #define RSC_NOALLOC_MAX_GATES 128

@@ -16,7 +16,7 @@
 #include <vector>
 
 #include "../../include/rsc.h"
-#include "rsc_pulse.cuh"
+#include "rsc_batch.cuh"
 
 using rsc::AdvanceArgs;
 using rsc::DebrisType;
@@ -97,6 +97,8 @@ struct rsc_worker {
     bool have_pulse_desc = false;
     float last_sim[16] = {0};
     uint64_t launches = 0;
+    /* pulse launch shape chosen by rsc_autotune (0: default) */
+    int tune_warps = 0, tune_per_sm = 0;
 };
 
 namespace {
@@ -229,31 +231,63 @@ int set_gates(rsc_worker *w) {
     return RSC_OK;
 }
 
-int pulse_geometry(rsc_worker *w, int mode, int *grid, int *threads, size_t *smem) {
-    size_t per_warp = rsc::pulse_warp_bytes(mode, w->G);
+template <typename K>
+cudaError_t kernel_occupancy(K kern, int threads, size_t smem, int *per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, threads, smem);
+    return e;
+}
+
+/* Launch shape of the pulse kernel (one-instance or batched form) for G
+ * gates: warps per block as many as fit 200 KB of bins (at most 16, at most
+ * want_warps when that is > 0), resident blocks per SM from the occupancy
+ * calculator (at most 4, at most want_per_sm when that is > 0). */
+int pulse_shape(int mode, bool batch, uint32_t G, int want_warps, int want_per_sm, int *per_sm_out, int *threads,
+                size_t *smem) {
+    size_t per_warp = rsc::pulse_warp_bytes(mode, G);
     size_t budget = 200 * 1024;
     int warps = (int)(budget / per_warp);
     if (warps > 16) warps = 16;
-    if (warps < 1) return fail(RSC_ERR_UNSUPPORTED, "%u gates do not fit the pulse kernel's shared memory", w->G);
+    if (warps < 1) return fail(RSC_ERR_UNSUPPORTED, "%u gates do not fit the pulse kernel's shared memory", G);
+    if (want_warps > 0 && want_warps < warps) warps = want_warps;
     *threads = warps * 32;
-    *smem = (size_t)warps * per_warp + 2 * w->G * sizeof(float);
+    *smem = (size_t)warps * per_warp + 2 * G * sizeof(float);
     int per_sm = 1;
     cudaError_t e;
     if (mode == RSC_PULSE_PLAIN) {
-        e = cudaFuncSetAttribute(rsc::k_pulse<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<0>, *threads, *smem);
+        e = batch ? kernel_occupancy(rsc::k_pulse_batch<0>, *threads, *smem, &per_sm)
+                  : kernel_occupancy(rsc::k_pulse<0>, *threads, *smem, &per_sm);
     } else if (mode == RSC_PULSE_COMPENSATED) {
-        e = cudaFuncSetAttribute(rsc::k_pulse<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<1>, *threads, *smem);
+        e = batch ? kernel_occupancy(rsc::k_pulse_batch<1>, *threads, *smem, &per_sm)
+                  : kernel_occupancy(rsc::k_pulse<1>, *threads, *smem, &per_sm);
     } else {
-        e = cudaFuncSetAttribute(rsc::k_pulse<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsc::k_pulse<2>, *threads, *smem);
+        e = batch ? kernel_occupancy(rsc::k_pulse_batch<2>, *threads, *smem, &per_sm)
+                  : kernel_occupancy(rsc::k_pulse<2>, *threads, *smem, &per_sm);
     }
     if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "pulse kernel configuration: %s", cudaGetErrorString(e));
     if (per_sm < 1) per_sm = 1;
     if (per_sm > 4) per_sm = 4;
+    if (want_per_sm > 0 && want_per_sm < per_sm) per_sm = want_per_sm;
+    *per_sm_out = per_sm;
+    return RSC_OK;
+}
+
+int pulse_geometry(rsc_worker *w, int mode, int *grid, int *threads, size_t *smem) {
+    int per_sm = 1;
+    int s = pulse_shape(mode, false, w->G, w->tune_warps, w->tune_per_sm, &per_sm, threads, smem);
+    if (s) return s;
     *grid = w->num_sms * per_sm;
     return RSC_OK;
+}
+
+void launch_pulse(int mode, const PulseArgs &P, int grid, int threads, size_t smem, cudaStream_t st) {
+    if (mode == RSC_PULSE_PLAIN) {
+        rsc::k_pulse<0><<<grid, threads, smem, st>>>(P);
+    } else if (mode == RSC_PULSE_COMPENSATED) {
+        rsc::k_pulse<1><<<grid, threads, smem, st>>>(P);
+    } else {
+        rsc::k_pulse<2><<<grid, threads, smem, st>>>(P);
+    }
 }
 
 void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
@@ -593,14 +627,14 @@ int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float 
     return RSC_OK;
 }
 
-int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const float sim_desc[16]) {
-    int s = check_alloc(w);
-    if (s) return s;
+/* The advance launch of one worker: descriptor and block count. */
+static int fill_advance_args(rsc_worker *w, const rsc_population *pop, int les_id, const float *sim_desc,
+                             AdvanceArgs &a, unsigned *blocks_out) {
     if (pop == nullptr || sim_desc == nullptr) return fail(RSC_ERR_ARG, "population / sim_desc is NULL");
     if (les_id < 0 || les_id > 1 || w->les_uvwt[les_id] == nullptr) return fail(RSC_ERR_STATE, "LES slot %d not set", les_id);
     if (pop->origins[0] + pop->counts[0] > w->num_scats) return fail(RSC_ERR_ARG, "background range beyond the arrays");
     const uint32_t concept = rsm_f2u(sim_desc[5]);
-    AdvanceArgs a;
+    int s;
     memset(&a, 0, sizeof(a));
     a.pos = w->pos;
     a.vel = w->vel;
@@ -634,7 +668,17 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
     s = fill_debris(w, pop, a, &deb);
     if (s) return s;
     if ((concept & rsc::kConceptDFF) && deb && a.dff == nullptr) return fail(RSC_ERR_STATE, "debris flux field not set");
-    unsigned blocks = a.rain_blocks + (unsigned)((deb + rsc::kAdvanceThreads - 1) / rsc::kAdvanceThreads);
+    *blocks_out = a.rain_blocks + (unsigned)((deb + rsc::kAdvanceThreads - 1) / rsc::kAdvanceThreads);
+    return RSC_OK;
+}
+
+int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const float sim_desc[16]) {
+    int s = check_alloc(w);
+    if (s) return s;
+    AdvanceArgs a;
+    unsigned blocks = 0;
+    s = fill_advance_args(w, pop, les_id, sim_desc, a, &blocks);
+    if (s) return s;
     if (blocks == 0) return RSC_OK;
     rsc::k_advance<<<blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
     RSC_CUDA(cudaGetLastError());
@@ -683,13 +727,7 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     }
     const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
     P.materialize = mat ? 1 : 0;
-    if (mode == RSC_PULSE_PLAIN) {
-        rsc::k_pulse<0><<<grid, threads, smem, w->stream>>>(P);
-    } else if (mode == RSC_PULSE_COMPENSATED) {
-        rsc::k_pulse<1><<<grid, threads, smem, w->stream>>>(P);
-    } else {
-        rsc::k_pulse<2><<<grid, threads, smem, w->stream>>>(P);
-    }
+    launch_pulse(mode, P, grid, threads, smem, w->stream);
     RSC_CUDA(cudaGetLastError());
     w->launches++;
     memcpy(w->last_sim, sim_desc, sizeof(w->last_sim));
@@ -741,6 +779,598 @@ int rsc_launch_count(rsc_worker *w, uint64_t *count) {
 int rsc_get_stream(rsc_worker *w, void **stream) {
     if (w == nullptr || stream == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
     *stream = (void *)w->stream;
+    return RSC_OK;
+}
+
+}  // extern "C"
+
+/* ---- launch-shape autotuning and the batching form ------------------------- */
+
+namespace {
+
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t init() {
+        cudaError_t e = cudaEventCreate(&a);
+        if (e == cudaSuccess) e = cudaEventCreate(&b);
+        return e;
+    }
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
+/* candidate shapes: warps per block x resident blocks per SM */
+const int kTuneWarps[] = {16, 8, 4};
+const int kTuneReps = 3;
+
+}  // namespace
+
+struct rsc_batch {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_join = nullptr, ev_h2d = nullptr, ev_done = nullptr;
+    std::vector<rsc_worker *> w;
+    std::vector<rsc_population> pops;
+    bool have_pops = false;
+    int mode = RSC_PULSE_PLAIN;
+    uint32_t Gmax = 0;
+    int tune_warps = 0, tune_per_sm = 0;
+    /* per-instance launch descriptors and block prefixes */
+    std::vector<rsc::BatchAdvance> h_adv;
+    std::vector<PulseArgs> h_pulse;
+    std::vector<unsigned> h_adv_prefix, h_pulse_prefix;
+    std::vector<uint32_t> concept;
+    rsc::BatchAdvance *d_adv = nullptr;
+    PulseArgs *d_pulse = nullptr;
+    unsigned *d_adv_prefix = nullptr, *d_pulse_prefix = nullptr;
+    unsigned adv_blocks = 0, pulse_blocks = 0;
+    int pulse_threads = 0, pulse_per_sm = 0;
+    size_t pulse_smem = 0;
+    /* per-step descriptors (pinned on the host) and the pulses of a run */
+    int cap_steps = 0;
+    rsc::BatchStep *h_steps = nullptr;
+    rsc::BatchStep *d_steps = nullptr;
+    float4 *d_out = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    uint64_t launches = 0;
+    /* LES refills on a copy stream: per instance and slot, the event of the
+     * last run that read the slot, the event of the refill's completion and
+     * whether a run still has to wait for it */
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> slot_used, slot_ready;
+    std::vector<char> slot_pending;
+};
+
+namespace {
+
+int check_batch(rsc_batch *b) {
+    if (b == nullptr) return fail(RSC_ERR_ARG, "batch is NULL");
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "cudaSetDevice(%d): %s", b->device, cudaGetErrorString(e));
+    return RSC_OK;
+}
+
+void batch_drop_graph(rsc_batch *b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_steps = 0;
+}
+
+/* Room for `steps` steps of per-step descriptors and pulses. */
+int batch_reserve(rsc_batch *b, int steps) {
+    if (steps <= b->cap_steps) return RSC_OK;
+    RSC_CUDA(cudaStreamSynchronize(b->stream));
+    batch_drop_graph(b);
+    if (b->h_steps) cudaFreeHost(b->h_steps);
+    free_ptr(b->d_steps);
+    free_ptr(b->d_out);
+    b->h_steps = nullptr;
+    b->d_steps = nullptr;
+    b->d_out = nullptr;
+    b->cap_steps = 0;
+    const size_t n = b->w.size();
+    const size_t rows = (size_t)steps * n;
+    cudaError_t e = cudaMallocHost((void **)&b->h_steps, rows * sizeof(rsc::BatchStep));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_steps, rows * sizeof(rsc::BatchStep));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_out, rows * b->Gmax * sizeof(float4));
+    if (e != cudaSuccess) return fail(RSC_ERR_NOMEM, "batch buffers for %d steps: %s", steps, cudaGetErrorString(e));
+    memset(b->h_steps, 0, rows * sizeof(rsc::BatchStep));
+    RSC_CUDA(cudaMemsetAsync(b->d_out, 0, rows * b->Gmax * sizeof(float4), b->stream));
+    b->cap_steps = steps;
+    return RSC_OK;
+}
+
+/* Build every instance's descriptors for the beam / concept of `row` (one
+ * BatchStep per instance) and the block prefixes; upload them.  A change of
+ * grid or block shape retires the captured graph. */
+int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
+    if (!b->have_pops) return fail(RSC_ERR_STATE, "rsc_batch_set_populations has not been called");
+    const size_t n = b->w.size();
+    int per_sm = 1, threads = 0;
+    size_t smem = 0;
+    int s = pulse_shape(b->mode, true, b->Gmax, b->tune_warps, b->tune_per_sm, &per_sm, &threads, &smem);
+    if (s) return s;
+    const double total = (double)b->num_sms * per_sm;
+    double sum_n = 0.0;
+    for (rsc_worker *x : b->w) sum_n += (double)x->num_scats;
+    b->h_adv.assign(n, rsc::BatchAdvance());
+    b->h_pulse.assign(n, PulseArgs());
+    b->h_adv_prefix.assign(n + 1, 0u);
+    b->h_pulse_prefix.assign(n + 1, 0u);
+    b->concept.assign(n, 0u);
+    unsigned acc_a = 0, acc_p = 0;
+    for (size_t i = 0; i < n; i++) {
+        rsc_worker *x = b->w[i];
+        if (x->pos == nullptr) return fail(RSC_ERR_STATE, "instance %zu is not allocated", i);
+        if (x->G > b->Gmax) return fail(RSC_ERR_STATE, "instance %zu has more gates than when the batch was created", i);
+        if (x->range_weight == nullptr || x->angular_weight == nullptr) {
+            return fail(RSC_ERR_STATE, "instance %zu: range / angular weight tables not set", i);
+        }
+        rsc::BatchAdvance &A = b->h_adv[i];
+        unsigned blocks = 0;
+        s = fill_advance_args(x, &b->pops[i], row[i].les_id, row[i].sim, A.a, &blocks);
+        if (s) {
+            char why[sizeof(g_err)];
+            snprintf(why, sizeof(why), "%s", g_err);
+            return fail(s, "instance %zu: %s", i, why);
+        }
+        for (int slot = 0; slot < 2; slot++) {
+            A.uvwt[slot] = make_image(x->les_uvwt[slot], x->les_nx, x->les_ny, x->les_nz);
+            A.cpxx[slot] = make_image(x->les_cpxx[slot], x->les_nx, x->les_ny, x->les_nz);
+            A.dff[slot] = x->dff[slot];
+        }
+        b->h_adv_prefix[i] = acc_a;
+        acc_a += blocks;
+        PulseArgs &P = b->h_pulse[i];
+        fill_pulse_args(x, P, row[i].sim);
+        if (b->mode == RSC_PULSE_COMPENSATED) P.rk = x->rk_hi;
+        P.materialize = 0;
+        /* pulse blocks in proportion to the scatterers, at least one, and no
+         * block without a scatterer to start on */
+        double share = sum_n > 0.0 ? total * (double)x->num_scats / sum_n : 1.0;
+        unsigned bi = (unsigned)llround(share);
+        unsigned cap = (unsigned)((x->num_scats + (size_t)threads - 1) / (size_t)threads);
+        if (bi > cap) bi = cap;
+        if (bi < 1) bi = 1;
+        b->h_pulse_prefix[i] = acc_p;
+        acc_p += bi;
+        b->concept[i] = rsm_f2u(row[i].sim[5]);
+    }
+    b->h_adv_prefix[n] = acc_a;
+    b->h_pulse_prefix[n] = acc_p;
+    if (acc_a != b->adv_blocks || acc_p != b->pulse_blocks || threads != b->pulse_threads || smem != b->pulse_smem) {
+        batch_drop_graph(b);
+    }
+    b->adv_blocks = acc_a;
+    b->pulse_blocks = acc_p;
+    b->pulse_threads = threads;
+    b->pulse_smem = smem;
+    b->pulse_per_sm = per_sm;
+    /* pageable sources: each copy has taken its bytes when the call returns */
+    RSC_CUDA(cudaMemcpyAsync(b->d_adv, b->h_adv.data(), n * sizeof(rsc::BatchAdvance), cudaMemcpyHostToDevice, b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_pulse, b->h_pulse.data(), n * sizeof(PulseArgs), cudaMemcpyHostToDevice, b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_adv_prefix, b->h_adv_prefix.data(), (n + 1) * sizeof(unsigned), cudaMemcpyHostToDevice,
+                             b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_pulse_prefix, b->h_pulse_prefix.data(), (n + 1) * sizeof(unsigned),
+                             cudaMemcpyHostToDevice, b->stream));
+    return RSC_OK;
+}
+
+cudaError_t batch_launch_pulse(rsc_batch *b, int k) {
+    const int n = (int)b->w.size();
+    const rsc::BatchStep *st = b->d_steps + (size_t)k * n;
+    float4 *out = b->d_out + (size_t)k * n * b->Gmax;
+    const unsigned g = b->pulse_blocks, t = (unsigned)b->pulse_threads;
+    const size_t sm = b->pulse_smem;
+    if (b->mode == RSC_PULSE_PLAIN) {
+        rsc::k_pulse_batch<0><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
+    } else if (b->mode == RSC_PULSE_COMPENSATED) {
+        rsc::k_pulse_batch<1><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
+    } else {
+        rsc::k_pulse_batch<2><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
+    }
+    return cudaGetLastError();
+}
+
+/* Steps 0..K-1: pulse of every instance, then the advance of every instance. */
+cudaError_t batch_enqueue(rsc_batch *b, int steps) {
+    const int n = (int)b->w.size();
+    for (int k = 0; k < steps; k++) {
+        cudaError_t e = batch_launch_pulse(b, k);
+        if (e != cudaSuccess) return e;
+        if (b->adv_blocks) {
+            rsc::k_advance_batch<<<b->adv_blocks, rsc::kAdvanceThreads, 0, b->stream>>>(
+                b->d_adv, b->d_steps + (size_t)k * n, b->d_adv_prefix, n);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
+}
+
+int batch_capture(rsc_batch *b, int steps) {
+    batch_drop_graph(b);
+    RSC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = batch_enqueue(b, steps);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        b->graph = nullptr;
+        return fail(RSC_ERR_CUDA, "graph capture of %d steps: %s", steps, cudaGetErrorString(e));
+    }
+    b->graph_steps = steps;
+    return RSC_OK;
+}
+
+/* Copy steps' descriptors into the pinned table, checking them. */
+int batch_fill_steps(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids) {
+    const size_t n = b->w.size();
+    RSC_CUDA(cudaEventSynchronize(b->ev_h2d));   /* the last run's copy of the table has been taken */
+    for (int k = 0; k < steps; k++) {
+        for (size_t i = 0; i < n; i++) {
+            const size_t r = (size_t)k * n + i;
+            const int les = les_ids ? les_ids[r] : 0;
+            rsc_worker *x = b->w[i];
+            if (les < 0 || les > 1 || x->les_uvwt[les] == nullptr) {
+                return fail(RSC_ERR_STATE, "step %d instance %zu: LES slot %d not set", k, i, les);
+            }
+            const float *sim = sim_descs + r * 16;
+            if (k > 0 && rsm_f2u(sim[5]) != rsm_f2u(sim_descs[i * 16 + 5])) {
+                return fail(RSC_ERR_ARG, "step %d instance %zu: the concept changes within a run", k, i);
+            }
+            const rsc_population &p = b->pops[i];
+            bool deb = false;
+            for (int t = 1; t < RSC_MAX_TYPES; t++) deb = deb || p.counts[t] != 0;
+            if ((rsm_f2u(sim[5]) & rsc::kConceptDFF) && deb && x->dff[les] == nullptr) {
+                return fail(RSC_ERR_STATE, "step %d instance %zu: debris flux field of slot %d not set", k, i, les);
+            }
+            rsc::BatchStep &S = b->h_steps[r];
+            memcpy(S.sim, sim, sizeof(S.sim));
+            S.les_id = les;
+        }
+    }
+    return RSC_OK;
+}
+
+/* Order the batch stream after every worker's queued work. */
+int batch_join_workers(rsc_batch *b) {
+    for (rsc_worker *x : b->w) {
+        RSC_CUDA(cudaEventRecord(b->ev_join, x->stream));
+        RSC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
+    }
+    return RSC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *blocks_per_sm_out) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (sim_desc == nullptr) return fail(RSC_ERR_ARG, "sim_desc is NULL");
+    if (w->range_weight == nullptr || w->angular_weight == nullptr) {
+        return fail(RSC_ERR_STATE, "range / angular weight tables not set");
+    }
+    const int mode = w->precision;
+    PulseArgs P;
+    fill_pulse_args(w, P, sim_desc);
+    if (mode == RSC_PULSE_COMPENSATED) P.rk = w->rk_hi;
+    P.materialize = 0;
+    EventPair ev;
+    RSC_CUDA(ev.init());
+    float best = INFINITY;
+    int best_w = 0, best_p = 0;
+    for (int warps : kTuneWarps) {
+        for (int per_sm = 1; per_sm <= 4; per_sm++) {
+            int got = 0, threads = 0;
+            size_t smem = 0;
+            s = pulse_shape(mode, false, w->G, warps, per_sm, &got, &threads, &smem);
+            if (s) return s;
+            if (threads != warps * 32 || got != per_sm) continue;   /* shape not reachable */
+            const int grid = w->num_sms * per_sm;
+            launch_pulse(mode, P, grid, threads, smem, w->stream);
+            RSC_CUDA(cudaEventRecord(ev.a, w->stream));
+            for (int r = 0; r < kTuneReps; r++) launch_pulse(mode, P, grid, threads, smem, w->stream);
+            RSC_CUDA(cudaEventRecord(ev.b, w->stream));
+            RSC_CUDA(cudaGetLastError());
+            RSC_CUDA(cudaEventSynchronize(ev.b));
+            float ms = 0.0f;
+            RSC_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+            w->launches += 1 + kTuneReps;
+            if (ms < best) {
+                best = ms;
+                best_w = warps;
+                best_p = per_sm;
+            }
+        }
+    }
+    w->tune_warps = best_w;
+    w->tune_per_sm = best_p;
+    memcpy(w->last_sim, sim_desc, sizeof(w->last_sim));
+    w->have_pulse_desc = true;
+    w->sig_aux_stale = true;
+    if (warps_out) *warps_out = best_w;
+    if (blocks_per_sm_out) *blocks_per_sm_out = best_p;
+    return RSC_OK;
+}
+
+int rsc_batch_create(rsc_worker *const *workers, int count, rsc_batch **out) {
+    if (out == nullptr || workers == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    if (count < 1) return fail(RSC_ERR_ARG, "batch of %d instances", count);
+    for (int i = 0; i < count; i++) {
+        if (workers[i] == nullptr) return fail(RSC_ERR_ARG, "instance %d is NULL", i);
+        if (workers[i]->pos == nullptr) return fail(RSC_ERR_STATE, "instance %d is not allocated", i);
+        if (workers[i]->device != workers[0]->device) return fail(RSC_ERR_ARG, "instances on different devices");
+        for (int j = 0; j < i; j++) {
+            if (workers[j] == workers[i]) return fail(RSC_ERR_ARG, "instance %d repeats instance %d", i, j);
+        }
+    }
+    rsc_batch *b = new rsc_batch();
+    b->device = workers[0]->device;
+    b->num_sms = workers[0]->num_sms;
+    b->w.assign(workers, workers + count);
+    b->pops.assign(count, rsc_population());
+    for (rsc_worker *x : b->w) b->Gmax = x->G > b->Gmax ? x->G : b->Gmax;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_h2d, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking);
+    b->slot_used.assign(2 * count, nullptr);
+    b->slot_ready.assign(2 * count, nullptr);
+    b->slot_pending.assign(2 * count, 0);
+    for (int q = 0; q < 2 * count && e == cudaSuccess; q++) {
+        e = cudaEventCreateWithFlags(&b->slot_used[q], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->slot_ready[q], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_adv, count * sizeof(rsc::BatchAdvance));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulse, count * sizeof(PulseArgs));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_adv_prefix, (count + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulse_prefix, (count + 1) * sizeof(unsigned));
+    if (e != cudaSuccess) {
+        rsc_batch_free(b);
+        return fail(RSC_ERR_CUDA, "batch creation: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return RSC_OK;
+}
+
+int rsc_batch_free(rsc_batch *b) {
+    if (b == nullptr) return RSC_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_drop_graph(b);
+    if (b->h_steps) cudaFreeHost(b->h_steps);
+    free_ptr(b->d_steps);
+    free_ptr(b->d_out);
+    free_ptr(b->d_adv);
+    free_ptr(b->d_pulse);
+    free_ptr(b->d_adv_prefix);
+    free_ptr(b->d_pulse_prefix);
+    if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
+    for (cudaEvent_t ev : b->slot_used) {
+        if (ev) cudaEventDestroy(ev);
+    }
+    for (cudaEvent_t ev : b->slot_ready) {
+        if (ev) cudaEventDestroy(ev);
+    }
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->ev_h2d) cudaEventDestroy(b->ev_h2d);
+    if (b->ev_done) cudaEventDestroy(b->ev_done);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return RSC_OK;
+}
+
+int rsc_batch_set_populations(rsc_batch *b, const rsc_population *pops) {
+    int s = check_batch(b);
+    if (s) return s;
+    if (pops == nullptr) return fail(RSC_ERR_ARG, "pops is NULL");
+    b->pops.assign(pops, pops + b->w.size());
+    b->have_pops = true;
+    return RSC_OK;
+}
+
+int rsc_batch_set_precision(rsc_batch *b, int mode) {
+    int s = check_batch(b);
+    if (s) return s;
+    if (mode != RSC_PULSE_PLAIN && mode != RSC_PULSE_COMPENSATED && mode != RSC_PULSE_F64) {
+        return fail(RSC_ERR_ARG, "precision mode %d", mode);
+    }
+    if (mode != b->mode) {
+        RSC_CUDA(cudaStreamSynchronize(b->stream));
+        batch_drop_graph(b);
+    }
+    b->mode = mode;
+    return RSC_OK;
+}
+
+int rsc_batch_autotune(rsc_batch *b, const float *sim_descs) {
+    int s = check_batch(b);
+    if (s) return s;
+    if (sim_descs == nullptr) return fail(RSC_ERR_ARG, "sim_descs is NULL");
+    s = batch_reserve(b, 1);
+    if (s) return s;
+    s = batch_fill_steps(b, 1, sim_descs, nullptr);
+    if (s) return s;
+    s = batch_join_workers(b);
+    if (s) return s;
+    const size_t n = b->w.size();
+    RSC_CUDA(cudaMemcpyAsync(b->d_steps, b->h_steps, n * sizeof(rsc::BatchStep), cudaMemcpyHostToDevice, b->stream));
+    RSC_CUDA(cudaEventRecord(b->ev_h2d, b->stream));
+    EventPair ev;
+    RSC_CUDA(ev.init());
+    float best = INFINITY;
+    int best_w = 0, best_p = 0;
+    for (int warps : kTuneWarps) {
+        for (int per_sm = 1; per_sm <= 4; per_sm++) {
+            b->tune_warps = warps;
+            b->tune_per_sm = per_sm;
+            s = batch_prepare(b, b->h_steps);
+            if (s) return s;
+            if (b->pulse_threads != warps * 32 || b->pulse_per_sm != per_sm) continue;
+            RSC_CUDA(batch_launch_pulse(b, 0));
+            RSC_CUDA(cudaEventRecord(ev.a, b->stream));
+            for (int r = 0; r < kTuneReps; r++) RSC_CUDA(batch_launch_pulse(b, 0));
+            RSC_CUDA(cudaEventRecord(ev.b, b->stream));
+            RSC_CUDA(cudaEventSynchronize(ev.b));
+            float ms = 0.0f;
+            RSC_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+            b->launches += 1 + kTuneReps;
+            if (ms < best) {
+                best = ms;
+                best_w = warps;
+                best_p = per_sm;
+            }
+        }
+    }
+    b->tune_warps = best_w;
+    b->tune_per_sm = best_p;
+    batch_drop_graph(b);
+    RSC_CUDA(cudaEventRecord(b->ev_done, b->stream));
+    for (rsc_worker *x : b->w) RSC_CUDA(cudaStreamWaitEvent(x->stream, b->ev_done, 0));
+    return RSC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids, float *pulses_out, int use_graph,
+              bool wait) {
+    int s = check_batch(b);
+    if (s) return s;
+    if (steps < 1) return fail(RSC_ERR_ARG, "steps %d", steps);
+    if (sim_descs == nullptr || les_ids == nullptr) return fail(RSC_ERR_ARG, "sim_descs / les_ids is NULL");
+    s = batch_reserve(b, steps);
+    if (s) return s;
+    s = batch_fill_steps(b, steps, sim_descs, les_ids);
+    if (s) return s;
+    s = batch_join_workers(b);
+    if (s) return s;
+    s = batch_prepare(b, b->h_steps);
+    if (s) return s;
+    const size_t n = b->w.size();
+    /* LES slots this run reads: wait for their pending refills */
+    std::vector<char> used(2 * n, 0);
+    for (size_t r = 0; r < (size_t)steps * n; r++) used[2 * (r % n) + (b->h_steps[r].les_id & 1)] = 1;
+    for (size_t q = 0; q < 2 * n; q++) {
+        if (used[q] && b->slot_pending[q]) {
+            RSC_CUDA(cudaStreamWaitEvent(b->stream, b->slot_ready[q], 0));
+            b->slot_pending[q] = 0;
+        }
+    }
+    RSC_CUDA(cudaMemcpyAsync(b->d_steps, b->h_steps, (size_t)steps * n * sizeof(rsc::BatchStep),
+                             cudaMemcpyHostToDevice, b->stream));
+    RSC_CUDA(cudaEventRecord(b->ev_h2d, b->stream));
+    if (use_graph) {
+        if (b->graph == nullptr || b->graph_steps != steps) {
+            s = batch_capture(b, steps);
+            if (s) return s;
+        }
+        RSC_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    } else {
+        RSC_CUDA(batch_enqueue(b, steps));
+    }
+    b->launches += (uint64_t)steps * (b->adv_blocks ? 2u : 1u);
+    for (size_t q = 0; q < 2 * n; q++) {
+        if (used[q]) RSC_CUDA(cudaEventRecord(b->slot_used[q], b->stream));
+    }
+    if (pulses_out) {
+        RSC_CUDA(cudaMemcpyAsync(pulses_out, b->d_out, (size_t)steps * n * b->Gmax * sizeof(float4),
+                                 cudaMemcpyDeviceToHost, b->stream));
+    }
+    RSC_CUDA(cudaEventRecord(b->ev_done, b->stream));
+    for (size_t i = 0; i < n; i++) {
+        rsc_worker *x = b->w[i];
+        RSC_CUDA(cudaStreamWaitEvent(x->stream, b->ev_done, 0));
+        memcpy(x->last_sim, sim_descs + ((size_t)(steps - 1) * n + i) * 16, sizeof(x->last_sim));
+        x->have_pulse_desc = true;
+        x->sig_aux_stale = true;
+    }
+    if (pulses_out && wait) RSC_CUDA(cudaStreamSynchronize(b->stream));
+    return RSC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsc_batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids, float *pulses_out,
+                  int use_graph) {
+    return batch_run(b, steps, sim_descs, les_ids, pulses_out, use_graph, true);
+}
+
+int rsc_batch_run_async(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids, float *pulses_out,
+                        int use_graph) {
+    return batch_run(b, steps, sim_descs, les_ids, pulses_out, use_graph, false);
+}
+
+int rsc_batch_synchronize(rsc_batch *b) {
+    int s = check_batch(b);
+    if (s) return s;
+    RSC_CUDA(cudaStreamSynchronize(b->stream));
+    RSC_CUDA(cudaStreamSynchronize(b->copy_stream));
+    return RSC_OK;
+}
+
+int rsc_batch_set_les_async(rsc_batch *b, int index, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx,
+                            uint32_t ny, uint32_t nz) {
+    int s = check_batch(b);
+    if (s) return s;
+    if (index < 0 || index >= (int)b->w.size()) return fail(RSC_ERR_ARG, "instance %d of %zu", index, b->w.size());
+    if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
+    if (uvwt4 == nullptr) return fail(RSC_ERR_ARG, "uvwt is NULL");
+    rsc_worker *x = b->w[index];
+    if (x->les_uvwt[slot] == nullptr || nx != x->les_nx || ny != x->les_ny || nz != x->les_nz) {
+        return fail(RSC_ERR_STATE, "instance %d: LES of %ux%ux%u not set with rsc_set_les", index, nx, ny, nz);
+    }
+    const size_t q = 2 * (size_t)index + slot;
+    const size_t bytes = (size_t)nx * ny * nz * sizeof(float4);
+    /* after the last batch run and any worker-stream work that read the slot */
+    RSC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->slot_used[q], 0));
+    RSC_CUDA(cudaEventRecord(b->ev_join, x->stream));
+    RSC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->ev_join, 0));
+    RSC_CUDA(cudaMemcpyAsync(x->les_uvwt[slot], uvwt4, bytes, cudaMemcpyHostToDevice, b->copy_stream));
+    if (cpxx4) RSC_CUDA(cudaMemcpyAsync(x->les_cpxx[slot], cpxx4, bytes, cudaMemcpyHostToDevice, b->copy_stream));
+    RSC_CUDA(cudaEventRecord(b->slot_ready[q], b->copy_stream));
+    b->slot_pending[q] = 1;
+    return RSC_OK;
+}
+
+int rsc_batch_max_gates(rsc_batch *b, int *max_gates) {
+    if (b == nullptr || max_gates == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *max_gates = (int)b->Gmax;
+    return RSC_OK;
+}
+
+int rsc_batch_launch_count(rsc_batch *b, uint64_t *count) {
+    if (b == nullptr || count == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *count = b->launches;
+    return RSC_OK;
+}
+
+int rsc_batch_get_stream(rsc_batch *b, void **stream) {
+    if (b == nullptr || stream == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *stream = (void *)b->stream;
+    return RSC_OK;
+}
+
+int rsc_batch_get_shape(rsc_batch *b, int *warps, int *blocks_per_sm) {
+    if (b == nullptr) return fail(RSC_ERR_ARG, "batch is NULL");
+    if (warps) *warps = b->tune_warps;
+    if (blocks_per_sm) *blocks_per_sm = b->tune_per_sm;
     return RSC_OK;
 }
 

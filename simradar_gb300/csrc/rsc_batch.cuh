@@ -1,0 +1,98 @@
+/*
+ * rsc_batch.cuh -- many emulation instances per launch.
+ *
+ * An instance is one worker: its own scatterer arrays, tables, gates, pulse
+ * accumulator and counter.  One time step of every instance is two launches:
+ * k_pulse_batch forms every instance's pulse, k_advance_batch advances every
+ * instance's scatterers.  Blocks are assigned to instances in proportion to
+ * their work through a prefix table; each block copies its instance's launch
+ * descriptor into shared memory, takes the step's beam / time / LES slot from
+ * the per-step table, and runs the same block bodies as the one-instance
+ * kernels (so every instance's state evolves bit for bit as it would alone).
+ * A run of K steps is 2 K launches whose arguments differ only in the step
+ * index, which is what lets the host capture it once in a CUDA graph.
+ */
+#ifndef SIMRADAR_GB300_RSC_BATCH_CUH
+#define SIMRADAR_GB300_RSC_BATCH_CUH
+
+#include "rsc_pulse.cuh"
+
+namespace rsc {
+
+/* per instance per step: the simulation descriptor and the LES slot */
+struct BatchStep {
+    float sim[16];
+    int les_id;
+    int pad[3];
+};
+
+/* per instance, fixed for the batch: the advance descriptor plus both LES /
+ * debris-flux-field slots (the step picks one) */
+struct BatchAdvance {
+    AdvanceArgs a;
+    Image uvwt[2], cpxx[2];
+    const float *dff[2];
+};
+
+/* the instance owning block b: the last i with prefix[i] <= b */
+__device__ __forceinline__ int batch_instance(const unsigned *prefix, int n, unsigned b) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= b) {
+            lo = mid;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    return lo;
+}
+
+/* copy `bytes` (a multiple of 4) from global to shared memory, whole block */
+__device__ __forceinline__ void block_copy(void *dst, const void *src, unsigned bytes) {
+    const unsigned *s = static_cast<const unsigned *>(src);
+    unsigned *d = static_cast<unsigned *>(dst);
+    for (unsigned k = threadIdx.x; k < bytes / 4; k += blockDim.x) d[k] = __ldg(s + k);
+}
+
+__global__ void __launch_bounds__(kAdvanceThreads, 4)
+k_advance_batch(const BatchAdvance *inst, const BatchStep *steps, const unsigned *prefix, int ninst) {
+    __shared__ __align__(16) AdvanceArgs sa;
+    __shared__ int s_i;
+    if (threadIdx.x == 0) s_i = batch_instance(prefix, ninst, blockIdx.x);
+    __syncthreads();
+    const int i = s_i;
+    block_copy(&sa, &inst[i].a, sizeof(AdvanceArgs));
+    __syncthreads();
+    if (threadIdx.x < 16) sa.sim[threadIdx.x] = steps[i].sim[threadIdx.x];
+    if (threadIdx.x == 0) {
+        const int les = steps[i].les_id & 1;
+        sa.uvwt = inst[i].uvwt[les];
+        sa.cpxx = inst[i].cpxx[les];
+        sa.dff = inst[i].dff[les];
+    }
+    __syncthreads();
+    advance_body(sa, blockIdx.x - __ldg(prefix + i));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(512)
+k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *prefix, int ninst, float4 *out,
+              unsigned out_stride) {
+    __shared__ __align__(16) PulseArgs sp;
+    __shared__ int s_i;
+    if (threadIdx.x == 0) s_i = batch_instance(prefix, ninst, blockIdx.x);
+    __syncthreads();
+    const int i = s_i;
+    block_copy(&sp, &inst[i], sizeof(PulseArgs));
+    __syncthreads();
+    if (threadIdx.x < 16) sp.sim[threadIdx.x] = steps[i].sim[threadIdx.x];
+    if (threadIdx.x == 0) sp.pulse = out + (size_t)i * out_stride;
+    __syncthreads();
+    const unsigned b0 = __ldg(prefix + i);
+    pulse_body<MODE>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
+}
+
+}  // namespace rsc
+
+#endif

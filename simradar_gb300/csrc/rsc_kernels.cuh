@@ -272,11 +272,9 @@ __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned lon
     return t;
 }
 
-/* 5 blocks of 256 per SM (<= 51 registers): the step is a chain of dependent
- * loads (state, then 8 LES texels, then the debris tables), so resident warps
- * are what hides the latency */
-__global__ void __launch_bounds__(kAdvanceThreads, 5) k_advance(const AdvanceArgs a) {
-    const unsigned b = blockIdx.x;
+/* block b of one time step: blocks [0, rain_blocks) take the background
+ * range, the rest the concatenated debris ranges */
+__device__ __forceinline__ void advance_body(const AdvanceArgs &a, unsigned b) {
     if (b < a.rain_blocks) {
         unsigned long long j = (unsigned long long)b * kAdvanceThreads + threadIdx.x;
         if (j >= a.rain_count) return;
@@ -295,6 +293,13 @@ __global__ void __launch_bounds__(kAdvanceThreads, 5) k_advance(const AdvanceArg
     int t = debris_type_of(a, j);
     const DebrisType &T = a.types[t];
     debris_step(a, T, (size_t)(T.origin + (j - a.deb_prefix[t])));
+}
+
+/* 5 blocks of 256 per SM (<= 51 registers): the step is a chain of dependent
+ * loads (state, then 8 LES texels, then the debris tables), so resident warps
+ * are what hides the latency */
+__global__ void __launch_bounds__(kAdvanceThreads, 5) k_advance(const AdvanceArgs a) {
+    advance_body(a, blockIdx.x);
 }
 
 /* ---- db_rcs (rs.cl:909-919) for every debris type ---- */

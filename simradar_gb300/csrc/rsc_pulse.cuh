@@ -173,8 +173,9 @@ __host__ __device__ constexpr size_t pulse_warp_bytes(int mode, unsigned G) {
                      : (mode == 1 ? (size_t)G * (32 + kBinStride32 * 4) : (size_t)G * 32);
 }
 
+/* block blk of the nblk blocks that form one pulse */
 template <int MODE>
-__global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
+__device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, unsigned nblk) {
     typedef PulseTraits<MODE> Tr;
     typedef typename Tr::Acc Acc;
     typedef typename Acc::bin_t bin_t;
@@ -196,11 +197,11 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     float *mini = mini_all + (size_t)warp * G * kBinStride32;
     float *fbins = (MODE == 1) ? mini : reinterpret_cast<float *>(wbins);   /* where FP32 atomics go */
 
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long stride = (unsigned long long)nblk * blockDim.x;
     const unsigned long long n = P.n;
     /* every lane of a warp runs the same number of iterations so the warp
      * collectives below see the full warp */
-    const unsigned long long base0 = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    const unsigned long long base0 = (unsigned long long)blk * blockDim.x + (threadIdx.x & ~31u);
     for (unsigned long long base = base0; base < n; base += stride) {
         const unsigned long long i = base + lane;
         const bool in = i < n;
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     __shared__ bool s_last;
     if (threadIdx.x == 0) {
         unsigned ticket = atomicAdd(P.counter, 1u);
-        s_last = (ticket == gridDim.x - 1);
+        s_last = (ticket == nblk - 1);
     }
     __syncthreads();
     if (!s_last) return;
@@ -405,6 +406,11 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
         P.acc64[o] = 0.0;
     }
     if (threadIdx.x == 0) *P.counter = 0u;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
+    pulse_body<MODE>(P, blockIdx.x, gridDim.x);
 }
 
 }  // namespace rsc

@@ -251,8 +251,19 @@ RSM_FN float rsm_asin_core(float s, float z) {
     return fmaf(s * z, p, s);
 }
 
+/* Every acos of the kernels takes a cosine formed from unit vectors or a unit
+ * quaternion (rs.cl:210, 327, 330, 485, 488, 855, 1066, 1451); rounding can
+ * carry it just past +-1, where the OpenCL builtin returns NaN and the NaN
+ * then reaches the scatterer's state and every range gate.  An argument
+ * within 16 ulp beyond +-1 is taken as +-1 here (a leaf whose relative wind
+ * lies along its body axis has beta = 0); inside [-1, 1], further out and
+ * for NaN nothing changes. */
 RSM_FN float rsm_acosf(float x) {
     float ax = fabsf(x);
+    if (ax > 1.0f && ax <= 0x1.00002p+0f) {
+        x = x > 0.0f ? 1.0f : -1.0f;
+        ax = 1.0f;
+    }
     if (rsm_isnan(x) || ax > 1.0f) {
         return (x - x) / (x - x);
     }

@@ -103,6 +103,20 @@ def load_library():
         "rsc_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
         "rsc_get_stream": ([P, ctypes.POINTER(P)], I),
         "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
+        "rsc_autotune": ([P, _f32p, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "rsc_batch_create": ([ctypes.POINTER(P), I, ctypes.POINTER(P)], I),
+        "rsc_batch_free": ([P], I),
+        "rsc_batch_set_populations": ([P, ctypes.POINTER(Population)], I),
+        "rsc_batch_set_precision": ([P, I], I),
+        "rsc_batch_autotune": ([P, _f32p], I),
+        "rsc_batch_run": ([P, I, _f32p, ctypes.POINTER(ctypes.c_int32), _f32p, I], I),
+        "rsc_batch_run_async": ([P, I, _f32p, ctypes.POINTER(ctypes.c_int32), _f32p, I], I),
+        "rsc_batch_synchronize": ([P], I),
+        "rsc_batch_set_les_async": ([P, I, I, _f32p, _f32p, U32, U32, U32], I),
+        "rsc_batch_max_gates": ([P, ctypes.POINTER(I)], I),
+        "rsc_batch_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
+        "rsc_batch_get_stream": ([P, ctypes.POINTER(P)], I),
+        "rsc_batch_get_shape": ([P, ctypes.POINTER(I), ctypes.POINTER(I)], I),
     }
     for name, (argtypes, restype) in sig.items():
         fn = getattr(lib, name)
@@ -301,4 +315,109 @@ class Worker:
     def stream(self):
         s = ctypes.c_void_p()
         _check(self._lib.rsc_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def autotune(self, sim_desc):
+        """Pick the pulse kernel's launch shape by timing (warps, blocks/SM)."""
+        d = f32(sim_desc)
+        wv, pv = ctypes.c_int(0), ctypes.c_int(0)
+        _check(self._lib.rsc_autotune(self._h, _fp(d), ctypes.byref(wv), ctypes.byref(pv)))
+        return wv.value, pv.value
+
+
+class Batch:
+    """Many workers stepped together: two launches per step for all of them
+    (the batching form of include/rsc.h).  Keeps references to the workers so
+    they outlive the batch."""
+
+    def __init__(self, workers):
+        self._lib = load_library()
+        self.workers = list(workers)
+        arr = (ctypes.c_void_p * len(self.workers))(*[w._h.value for w in self.workers])
+        h = ctypes.c_void_p()
+        _check(self._lib.rsc_batch_create(arr, len(self.workers), ctypes.byref(h)))
+        self._h = h
+        g = ctypes.c_int(0)
+        _check(self._lib.rsc_batch_max_gates(self._h, ctypes.byref(g)))
+        self.max_gates = g.value
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rsc_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_populations(self, pops):
+        arr = (Population * len(self.workers))(*pops)
+        _check(self._lib.rsc_batch_set_populations(self._h, arr))
+
+    def set_precision(self, mode):
+        _check(self._lib.rsc_batch_set_precision(self._h, int(mode)))
+
+    def autotune(self, sim_descs):
+        d = f32(sim_descs).reshape(len(self.workers), 16)
+        _check(self._lib.rsc_batch_autotune(self._h, _fp(d)))
+        return self.shape
+
+    @property
+    def shape(self):
+        wv, pv = ctypes.c_int(0), ctypes.c_int(0)
+        _check(self._lib.rsc_batch_get_shape(self._h, ctypes.byref(wv), ctypes.byref(pv)))
+        return wv.value, pv.value
+
+    def run(self, sim_descs, les_ids=None, out=None, use_graph=True, download=True, wait=True):
+        """sim_descs: (steps, instances, 16).  Returns (steps, instances,
+        max_gates, 4) pulses (no gain) when download is set.  With wait False
+        the call returns once the work is queued; `out` (page-locked for an
+        asynchronous copy) is filled by the time synchronize() returns."""
+        d = f32(sim_descs)
+        steps = d.shape[0]
+        d = d.reshape(steps, len(self.workers), 16)
+        if les_ids is None:
+            les = np.zeros((steps, len(self.workers)), dtype=np.int32)
+        else:
+            les = np.ascontiguousarray(les_ids, dtype=np.int32).reshape(steps, len(self.workers))
+        if download and out is None:
+            out = np.empty((steps, len(self.workers), self.max_gates, 4), dtype=np.float32)
+        fn = self._lib.rsc_batch_run if wait else self._lib.rsc_batch_run_async
+        _check(fn(self._h, int(steps), _fp(d), les.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                  _fp(out) if download else None, 1 if use_graph else 0))
+        return out if download else None
+
+    def synchronize(self):
+        _check(self._lib.rsc_batch_synchronize(self._h))
+        self._keep = []
+
+    def set_les_async(self, index, slot, uvwt, cpxx=None):
+        """Refill an instance's LES slot on the batch's copy stream (the
+        arrays must stay alive, and should be page-locked, until
+        synchronize())."""
+        u = f32(uvwt)
+        c = f32(cpxx) if cpxx is not None else None
+        nz, ny, nx = u.shape[:3]
+        self._keep.append((u, c))
+        _check(self._lib.rsc_batch_set_les_async(self._h, int(index), int(slot), _fp(u), _fp(c), nx, ny, nz))
+
+    @property
+    def launch_count(self):
+        n = ctypes.c_uint64(0)
+        _check(self._lib.rsc_batch_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(self._lib.rsc_batch_get_stream(self._h, ctypes.byref(s)))
         return s.value or 0

@@ -352,13 +352,16 @@ def rhi_positions(az, el0, el1, delv):
 
 def make_scene(num_rain=131072, debris=(), gate_spacing=15.0, gates=None, range_start=None, seed=19760520,
                les_cfg=None, les_count=2, concept=CONCEPT_DBU, scan=None, lam=0.1, prt=1.0e-3, tau=0.2e-6,
-               beamwidth=1.0, dsd_diameters=None, box=None, gate_offset=0.0, les_seed=1, with_tables=True):
+               beamwidth=1.0, dsd_diameters=None, box=None, range_offset=0.0, les_seed=1, with_tables=True,
+               dsd_n0=8000.0):
     """A synthetic scene with the geometry of the reference's default box:
     R 1850-2420 m, azimuth +-8 deg, elevation 0-18 deg (RS_suggest_scan_domain
     for the suctvort LES, rs.c:5850-5877).  Positions are uniform in the box;
     seeds are uniform 31-bit integers.  `debris` is a list of (obj, count).
-    `gate_offset` moves the gates (not the scatterers) outward, the
-    30 km stress case of the precision form."""
+    `range_offset` moves the box (and the LES domain, which is centred on it)
+    and the gates that far along +y: the 30 km case of the precision form,
+    where the two-way phase 4 pi r / lambda is ~4e6 rad and one FP32 ulp of r
+    is 2 mm.  `dsd_n0` is the Marshall-Palmer intercept (m^-3 mm^-1)."""
     S = Scene()
     rng = np.random.default_rng(seed)
     c = F(3.0e8)
@@ -377,21 +380,21 @@ def make_scene(num_rain=131072, debris=(), gate_spacing=15.0, gates=None, range_
         X = R * np.cos(E) * np.sin(A)
         Y = R * np.cos(E) * np.cos(A)
         Z = R * np.sin(E)
-        box = (X.min(), Y.min(), Z.min(), X.max() - X.min(), Y.max() - Y.min(), Z.max() - Z.min())
+        box = (X.min(), Y.min() + range_offset, Z.min(), X.max() - X.min(), Y.max() - Y.min(), Z.max() - Z.min())
     S.box = tuple(float(F(v)) for v in box)
     ox, oy, oz, sx, sy, sz = S.box
     if range_start is None:
         range_start = 1850.0
     if gates is None:
         gates = int(round((2420.0 - 1850.0) / gate_spacing)) + 2
-    S.range_start = F(range_start + gate_offset)
+    S.range_start = F(range_start + range_offset)
     S.range_delta = F(gate_spacing)
     S.range_count = int(gates)
     S.dr = dr
     # DSD
     if dsd_diameters is None:
         dsd_diameters = np.arange(1, 11) * 0.5e-3
-    S.dsd_r, S.dsd_pdf, S.dsd_cdf, S.dsd_nd = marshall_palmer(dsd_diameters)
+    S.dsd_r, S.dsd_pdf, S.dsd_cdf, S.dsd_nd = marshall_palmer(dsd_diameters, n0=dsd_n0)
     # population
     counts = [int(num_rain)] + [int(n) for _, n in debris]
     S.num_scats = int(sum(counts))

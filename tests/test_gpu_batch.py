@@ -1,0 +1,211 @@
+"""GPU parity of the batching form: many instances stepped by two launches per
+step (one pulse launch and one advance launch for all of them), with and
+without a CUDA graph.
+
+Every instance must evolve bit for bit as the oracle does for it alone, and
+its pulses must agree with the exact FP32 sum within the same bound as the
+one-instance path (PULSE_TOL of test_gpu_parity).
+"""
+import numpy as np
+import pytest
+
+from simradar_gb300 import synth
+
+from test_gpu_parity import (STATE_FIELDS, assert_comp_close, assert_pulse_close, assert_state_equal, bits,
+                             push_to_edges)
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    """Uneven instances: sizes from 1 to 20k, different debris mixes, gate
+    counts, scans and concepts (one scene's LES volumes shared by all)."""
+    A = synth.make_scene(num_rain=20000, debris=[(synth.OBJ_LEAF, 256), (synth.OBJ_WOODBOARD_2X4, 256),
+                                                 (synth.OBJ_BRICK, 256)], les_count=2, seed=11)
+    push_to_edges(A)
+    B = synth.make_scene(num_rain=3000, gates=24, gate_spacing=20.0, concept=0, with_tables=False, seed=12,
+                         scan=synth.rhi_positions(2.0, 0.5, 20.0, 0.5))
+    C = synth.make_scene(num_rain=1, with_tables=False, seed=13)
+    D = synth.make_scene(num_rain=65, debris=[(synth.OBJ_BRICK, 1000)], with_tables=False, seed=14,
+                         concept=synth.CONCEPT_DRAGGED | synth.CONCEPT_CROSS_POL)
+    for S in (B, C, D):
+        S.les, S.les_cfg, S.les_desc = A.les, A.les_cfg, A.les_desc
+    return [A, B, C, D]
+
+
+@pytest.fixture(scope="module")
+def scenes():
+    return _scenes()
+
+
+def _workers(backend, scenes, precision=0):
+    ws = []
+    for S in scenes:
+        W = backend.Worker(0)
+        synth.load_worker(W, S)
+        W.set_precision(precision)
+        ws.append(W)
+    return ws
+
+
+def _steps(scenes, k0, count, les_of=lambda k: 0):
+    sims = np.zeros((count, len(scenes), 16), np.float32)
+    les = np.zeros((count, len(scenes)), np.int32)
+    for j in range(count):
+        k = k0 + j
+        for i, S in enumerate(scenes):
+            sims[j, i] = synth.pulse_sim_desc(S, k + i, tic=k * 1e-3)
+            les[j, i] = les_of(k)
+    return sims, les
+
+
+def test_batch_matches_oracle(backend, oracle_lib, scenes):
+    """Six steps in two graph runs of three, with a LES slot swap in the
+    second: state bit-exact and pulses within the summation bound, for every
+    instance."""
+    O = oracle_lib
+    ws = _workers(backend, scenes)
+    B = backend.Batch(ws)
+    B.set_populations([synth.population(S) for S in scenes])
+    sts = [O.OracleState(S.state) for S in scenes]
+    les_of = lambda k: 0 if k < 4 else 1
+    for k0 in (0, 3):
+        sims, les = _steps(scenes, k0, 3, les_of)
+        pulses = B.run(sims, les, use_graph=True)
+        for j in range(3):
+            for i, S in enumerate(scenes):
+                sd = sims[j, i]
+                direct, ab = O.make_pulse_direct(sts[i], S, sd, return_abs=True)
+                g = pulses[j, i, :S.range_count]
+                assert np.isfinite(g).all()
+                assert_pulse_close(g, direct, ab, "instance %d step %d" % (i, k0 + j))
+                O.advance_time(sts[i], S, S.counts, S.les[les[j, i]], sd)
+        for i, W in enumerate(ws):
+            assert_state_equal(W.download(STATE_FIELDS), sts[i].s, where="instance %d after step %d " % (i, k0 + 2))
+    assert B.launch_count == 12
+    # respawns happened in the big instance and were reproduced
+    assert (bits(sts[0].s["rnd"]) != bits(scenes[0].state["rnd"])).any(axis=1).sum() >= 64
+    B.close()
+    for W in ws:
+        W.close()
+
+
+def test_batch_les_refill(backend, oracle_lib, scenes):
+    """An LES slot refilled on the copy stream between runs is what the next
+    run that reads it sees: slot 1 is refilled with volume 0 while the
+    instances step on slot 0, then they step on slot 1."""
+    O = oracle_lib
+    sub = [scenes[0], scenes[3]]
+    ws = _workers(backend, sub)
+    B = backend.Batch(ws)
+    B.set_populations([synth.population(S) for S in sub])
+    sts = [O.OracleState(S.state) for S in sub]
+    sims, les = _steps(sub, 0, 2)
+    B.run(sims, les, download=False, wait=False)
+    v = sub[0].les[0]
+    for i in range(len(sub)):
+        B.set_les_async(i, 1, v.uvwt, v.cpxx)
+    sims2, les2 = _steps(sub, 2, 2, les_of=lambda k: 1)
+    B.run(sims2, les2)
+    B.synchronize()
+    for i, S in enumerate(sub):
+        for j in range(2):
+            O.advance_time(sts[i], S, S.counts, S.les[0], sims[j, i])
+        for j in range(2):
+            O.advance_time(sts[i], S, S.counts, S.les[0], sims2[j, i])
+        assert_state_equal(ws[i].download(STATE_FIELDS), sts[i].s, where="instance %d " % i)
+    B.close()
+    for W in ws:
+        W.close()
+
+
+def test_batch_graph_equals_stream(backend, scenes):
+    """The captured graph and the stream-ordered launches give the same state
+    bit for bit, and the same pulses within the summation bound."""
+    wa = _workers(backend, scenes)
+    wb = _workers(backend, scenes)
+    Ba, Bb = backend.Batch(wa), backend.Batch(wb)
+    pops = [synth.population(S) for S in scenes]
+    Ba.set_populations(pops)
+    Bb.set_populations(pops)
+    for k0 in (0, 2, 4):
+        sims, les = _steps(scenes, k0, 2)
+        pa = Ba.run(sims, les, use_graph=True)
+        pb = Bb.run(sims, les, use_graph=False)
+        scale = np.abs(pb).max(axis=(2, 3), keepdims=True) + 1e-30
+        assert np.all(np.abs(pa - pb) <= 1e-4 * scale)
+    for x, y in zip(wa, wb):
+        sa, sb = x.download(STATE_FIELDS), y.download(STATE_FIELDS)
+        for f in STATE_FIELDS:
+            assert np.array_equal(bits(sa[f]), bits(sb[f])), f
+    for o in [Ba, Bb] + wa + wb:
+        o.close()
+
+
+def test_batch_autotune_and_compensated(backend, oracle_lib, scenes):
+    """The autotuner picks a reachable shape and leaves the state alone; the
+    compensated form in a batch keeps its bound against FP64."""
+    O = oracle_lib
+    ws = _workers(backend, scenes, precision=1)
+    B = backend.Batch(ws)
+    B.set_populations([synth.population(S) for S in scenes])
+    B.set_precision(1)
+    sims, les = _steps(scenes, 0, 2)
+    warps, per_sm = B.autotune(sims[0])
+    assert warps in (4, 8, 16) and 1 <= per_sm <= 4
+    for i, W in enumerate(ws):
+        assert_state_equal(W.download(STATE_FIELDS), scenes[i].state, where="instance %d after autotune " % i)
+    sts = [O.OracleState(S.state) for S in scenes]
+    pulses = B.run(sims, les)
+    for j in range(2):
+        for i, S in enumerate(scenes):
+            r64, ab = O.make_pulse_f64(sts[i], S, sims[j, i], return_abs=True)
+            assert_comp_close(pulses[j, i, :S.range_count], r64, ab, "instance %d step %d" % (i, j))
+            O.advance_time(sts[i], S, S.counts, S.les[0], sims[j, i])
+    for i, W in enumerate(ws):
+        assert_state_equal(W.download(STATE_FIELDS), sts[i].s, where="instance %d " % i)
+    B.close()
+    for W in ws:
+        W.close()
+
+
+def test_worker_autotune(backend, scenes):
+    S = scenes[0]
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    sd = synth.pulse_sim_desc(S, 0)
+    W.make_pulse(sd)
+    ref = W.download_pulse(1.0)
+    warps, per_sm = W.autotune(sd)
+    assert warps in (4, 8, 16) and 1 <= per_sm <= 4
+    W.make_pulse(sd)
+    g = W.download_pulse(1.0)
+    assert np.all(np.abs(g - ref) <= 1e-4 * np.abs(ref).max())
+    assert_state_equal(W.download(STATE_FIELDS), S.state, where="after autotune ")
+    W.close()
+
+
+def test_batch_errors(backend, scenes):
+    """Bad descriptors are refused with a status, before any launch."""
+    ws = _workers(backend, scenes[1:3])
+    B = backend.Batch(ws)
+    sims, les = _steps(scenes[1:3], 0, 2)
+    with pytest.raises(backend.BackendError):   # populations not set
+        B.run(sims, les)
+    B.set_populations([synth.population(S) for S in scenes[1:3]])
+    bad = les.copy()
+    bad[1, 0] = 2                               # no such LES slot
+    with pytest.raises(backend.BackendError):
+        B.run(sims, bad)
+    bad_sims = sims.copy()
+    bad_sims[1, 1, 5] = synth.fbits(synth.CONCEPT_FIXED_POS)   # concept changes within the run
+    with pytest.raises(backend.BackendError):
+        B.run(bad_sims, les)
+    with pytest.raises(backend.BackendError):
+        B.set_precision(7)
+    with pytest.raises(backend.BackendError):
+        backend.Batch([ws[0], ws[0]])
+    assert B.launch_count == 0
+    B.close()
+    for W in ws:
+        W.close()

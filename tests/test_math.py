@@ -66,3 +66,17 @@ def test_special_inputs(oracle_lib):
     assert oracle_lib.eval_math(3, np.array([1e-30], np.float32))[0] == np.float32(1e-30)
     assert np.isnan(oracle_lib.eval_math(0, np.array([np.inf], np.float32)))[0]
     assert oracle_lib.eval_math(6, np.array([-200.0, 200.0], np.float32)).tolist() == [0.0, np.inf]
+
+
+def test_acos_domain_edge(oracle_lib):
+    """A cosine that rounding carried just past +-1 (u_hat.x = 1.00000012 was
+    met by a leaf in a 33.5M-scatterer run, rs.cl:210) is taken as +-1, not
+    NaN, up to 16 ulp out; beyond that, and NaN, still give NaN."""
+    one = np.float32(1.0)
+    a = np.array([1.0, np.nextafter(one, np.float32(2.0)), one + np.float32(16 * 2.0 ** -23), -1.0,
+                  -np.nextafter(one, np.float32(2.0)), one + np.float32(17 * 2.0 ** -23), np.nan],
+                 dtype=np.float32)
+    got = oracle_lib.eval_math(4, a)
+    assert got[0] == 0.0 and got[1] == 0.0 and got[2] == 0.0
+    assert abs(float(got[3]) - np.pi) < 1e-6 and got[4] == got[3]
+    assert np.isnan(got[5]) and np.isnan(got[6])
