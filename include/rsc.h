@@ -171,6 +171,17 @@ int rsc_launch_count(rsc_worker *w, uint64_t *count);
  * time with events on it). */
 int rsc_get_stream(rsc_worker *w, void **stream);
 
+/* ---- spatial order (additive) ----
+ * The worker keeps its background scatterers (type 0) in Morton order of
+ * their cell in the scan box, restored by a counting sort after every
+ * `steps` calls of rsc_advance_time (and after an upload of positions); 0
+ * keeps the caller's order.  The order is invisible at the ABI: upload and
+ * download map the caller's indices, and no result depends on it beyond the
+ * rounding of the gate sums.  Default 128. */
+int rsc_set_sort_interval(rsc_worker *w, int steps);
+/* Number of sorts the worker has made. */
+int rsc_sort_count(rsc_worker *w, uint64_t *count);
+
 /* ---- launch-shape autotuning (additive) ----
  * Time the pulse kernel of this worker at each candidate shape (warps per
  * block 4 / 8 / 16 and 1-4 resident blocks per SM) on the current state and

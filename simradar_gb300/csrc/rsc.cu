@@ -17,6 +17,7 @@
 
 #include "../../include/rsc.h"
 #include "rsc_batch.cuh"
+#include "rsc_sort.cuh"
 
 using rsc::AdvanceArgs;
 using rsc::DebrisType;
@@ -99,6 +100,15 @@ struct rsc_worker {
     uint64_t launches = 0;
     /* pulse launch shape chosen by rsc_autotune (0: default) */
     int tune_warps = 0, tune_per_sm = 0;
+    /* spatial order of the background range (rsc_sort.cuh): perm[slot] is the
+     * caller's index, inv[index] the slot; NULL perm = caller's order */
+    int sort_interval = 128;
+    uint64_t since_sort = 0;
+    bool sort_due = true;
+    unsigned *perm = nullptr, *perm_alt = nullptr, *inv = nullptr;
+    unsigned *sort_key = nullptr, *sort_order = nullptr, *sort_hist = nullptr, *sort_blocks = nullptr;
+    uint4 *alt[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint64_t sorts = 0;
 };
 
 namespace {
@@ -121,6 +131,32 @@ void free_ptr(void *p) {
     if (p) cudaFree(p);
 }
 
+void free_sort(rsc_worker *w) {
+    unsigned **u[] = {&w->perm, &w->perm_alt, &w->inv, &w->sort_key, &w->sort_order, &w->sort_hist, &w->sort_blocks};
+    for (unsigned **q : u) {
+        free_ptr(*q);
+        *q = nullptr;
+    }
+    for (uint4 *&a : w->alt) {
+        free_ptr(a);
+        a = nullptr;
+    }
+    w->sort_due = true;
+    w->since_sort = 0;
+}
+
+/* The eight attribute arrays as 16-byte elements, in a fixed order. */
+void attribute_arrays(rsc_worker *w, uint4 **out[8]) {
+    out[0] = reinterpret_cast<uint4 **>(&w->pos);
+    out[1] = reinterpret_cast<uint4 **>(&w->vel);
+    out[2] = reinterpret_cast<uint4 **>(&w->ori);
+    out[3] = reinterpret_cast<uint4 **>(&w->tum);
+    out[4] = reinterpret_cast<uint4 **>(&w->aux);
+    out[5] = reinterpret_cast<uint4 **>(&w->rcs);
+    out[6] = reinterpret_cast<uint4 **>(&w->sig);
+    out[7] = &w->rnd;
+}
+
 void free_arrays(rsc_worker *w) {
     free_ptr(w->pos);
     free_ptr(w->vel);
@@ -138,6 +174,7 @@ void free_arrays(rsc_worker *w) {
     free_ptr(w->rk64);
     free_ptr(w->acc64);
     free_ptr(w->counter);
+    free_sort(w);
     w->pos = w->vel = w->ori = w->tum = w->aux = w->rcs = w->sig = w->pulse = nullptr;
     w->rnd = nullptr;
     w->pulse64 = nullptr;
@@ -313,6 +350,7 @@ void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
     memcpy(P.rwv, w->range_weight_small, sizeof(P.rwv));
     P.acc64 = w->acc64;
     P.counter = w->counter;
+    P.coherent_span = w->perm != nullptr ? (int)w->G + 1 : 0;
     P.pulse = w->pulse;
     P.pulse64 = w->pulse64;
     /* Candidate window of the sparse path.  The weight is W[0] or W[xm] when
@@ -585,20 +623,165 @@ int rsc_set_dff(rsc_worker *w, int slot, const float *icdf, uint32_t n, const fl
     return RSC_OK;
 }
 
+static unsigned grid_of(unsigned long long n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
+
+/* Counting sort of the background range into spatial order: range shells
+ * of a quarter gate, then Morton order of direction, over the scan box
+ * (sim_desc s8-s10 origin, s12-s14 size): rsc_sort.cuh.  Every
+ * attribute array and perm move to the second buffer set, which then becomes
+ * the current one. */
+static int sort_worker(rsc_worker *w, const rsc_population *pop, const float *sim, cudaStream_t st) {
+    const unsigned long long origin = pop->origins[0], count = pop->counts[0];
+    w->sort_due = false;
+    w->since_sort = 0;
+    if (count < 256 || origin + count > w->num_scats) return RSC_OK;
+    const unsigned long long numel = w->numel;
+    if (w->perm == nullptr) {
+        const size_t u4 = numel * sizeof(unsigned);
+        cudaError_t e = cudaMalloc((void **)&w->perm, u4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&w->perm_alt, u4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&w->inv, u4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&w->sort_key, u4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&w->sort_order, u4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&w->sort_hist, sizeof(unsigned) * rsc::kMaxSortCells);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&w->sort_blocks, sizeof(unsigned) * rsc::kScanBlock);
+        for (int k = 0; k < 8 && e == cudaSuccess; k++) e = cudaMalloc((void **)&w->alt[k], numel * sizeof(uint4));
+        if (e != cudaSuccess) {
+            free_sort(w);
+            w->sort_due = false;
+            return fail(RSC_ERR_NOMEM, "spatial-order buffers for %llu scatterers: %s", numel, cudaGetErrorString(e));
+        }
+        rsc::k_iota<<<grid_of(numel, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(w->perm, numel);
+        rsc::k_iota<<<grid_of(numel, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(w->inv, numel);
+        w->launches += 2;
+    }
+    /* range shells of a quarter gate over the box's range, direction cells
+     * over its direction cosines, about one scatterer per cell, at most
+     * kMaxSortCells cells */
+    double r_lo = INFINITY, r_hi = 0.0, u_lo = INFINITY, u_hi = -INFINITY, v_lo = INFINITY, v_hi = -INFINITY;
+    for (int c = 0; c < 8; c++) {
+        const double x = (double)sim[8] + ((c & 1) ? (double)sim[12] : 0.0);
+        const double y = (double)sim[9] + ((c & 2) ? (double)sim[13] : 0.0);
+        const double z = (double)sim[10] + ((c & 4) ? (double)sim[14] : 0.0);
+        const double r = sqrt(x * x + y * y + z * z);
+        if (!(r > 0.0)) continue;
+        r_lo = fmin(r_lo, r);
+        r_hi = fmax(r_hi, r);
+        u_lo = fmin(u_lo, x / r);
+        u_hi = fmax(u_hi, x / r);
+        v_lo = fmin(v_lo, z / r);
+        v_hi = fmax(v_hi, z / r);
+    }
+    if (!(r_hi > r_lo) || !(u_hi > u_lo) || !(v_hi > v_lo)) {
+        r_lo = 0.0, r_hi = 1.0, u_lo = -1.0, u_hi = 1.0, v_lo = -1.0, v_hi = 1.0;
+    }
+    double shell = fabs((double)w->range_delta) * 0.25;
+    if (!(shell > 0.0)) shell = (r_hi - r_lo) / 64.0;
+    double shells_d = ceil((r_hi - r_lo) / shell);
+    if (shells_d < 1.0) shells_d = 1.0;
+    if (shells_d > (double)(rsc::kMaxSortCells / 4)) shells_d = (double)(rsc::kMaxSortCells / 4);
+    const unsigned shells = (unsigned)shells_d;
+    unsigned bits = (unsigned)lrint(0.5 * log2(fmax((double)count / shells, 1.0)));
+    if (bits > 12) bits = 12;
+    while (bits > 0 && ((unsigned long long)shells << (2 * bits)) > rsc::kMaxSortCells) bits--;
+    const unsigned H = shells << (2 * bits);
+    RSC_CUDA(cudaMemsetAsync(w->sort_hist, 0, H * sizeof(unsigned), st));
+    rsc::SortArgs a;
+    a.pos = w->pos;
+    a.origin = origin;
+    a.count = count;
+    a.r0 = (float)r_lo;
+    a.ir = (float)(1.0 / (shells * shell));
+    a.u0 = (float)u_lo;
+    a.iu = (float)(1.0 / (u_hi - u_lo));
+    a.v0 = (float)v_lo;
+    a.iv = (float)(1.0 / (v_hi - v_lo));
+    a.shells = shells;
+    a.bits = bits;
+    a.key = w->sort_key;
+    a.hist = w->sort_hist;
+    rsc::k_sort_key<<<grid_of(count, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(a);
+    const unsigned nb = (H + rsc::kScanBlock - 1) / rsc::kScanBlock;
+    rsc::k_scan_blocks<<<nb, rsc::kScanThreads, 0, st>>>(w->sort_hist, H, w->sort_blocks);
+    rsc::k_scan_top<<<1, rsc::kScanThreads, 0, st>>>(w->sort_blocks, nb);
+    rsc::k_scan_add<<<nb, rsc::kScanThreads, 0, st>>>(w->sort_hist, H, w->sort_blocks);
+    rsc::k_sort_scatter<<<grid_of(count, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(w->sort_key, count,
+                                                                                        w->sort_hist, w->sort_order);
+    uint4 **arr[8];
+    attribute_arrays(w, arr);
+    rsc::PermuteArgs p;
+    for (int k = 0; k < 8; k++) {
+        p.src[k] = *arr[k];
+        p.dst[k] = w->alt[k];
+    }
+    p.perm_src = w->perm;
+    p.perm_dst = w->perm_alt;
+    p.origin = origin;
+    p.count = count;
+    p.numel = numel;
+    p.order = w->sort_order;
+    rsc::k_sort_permute<<<grid_of(numel, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(p);
+    for (int k = 0; k < 8; k++) {
+        uint4 *t = *arr[k];
+        *arr[k] = w->alt[k];
+        w->alt[k] = t;
+    }
+    unsigned *t = w->perm;
+    w->perm = w->perm_alt;
+    w->perm_alt = t;
+    rsc::k_sort_inverse<<<grid_of(numel, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(w->perm, w->inv, numel);
+    RSC_CUDA(cudaGetLastError());
+    w->launches += 8;
+    w->sorts++;
+    return RSC_OK;
+}
+
+/* Sort when the interval has passed or the state was replaced. */
+static int maybe_sort(rsc_worker *w, const rsc_population *pop, const float *sim, cudaStream_t st) {
+    if (w->sort_interval <= 0) return RSC_OK;
+    if (!w->sort_due && w->since_sort < (uint64_t)w->sort_interval) return RSC_OK;
+    return sort_worker(w, pop, sim, st);
+}
+
 int rsc_upload(rsc_worker *w, size_t offset, size_t count, const float *pos4, const float *vel4, const float *ori4,
                const float *tum4, const float *aux4, const float *rcs4, const float *sig4, const uint32_t *rnd4) {
     int s = check_alloc(w);
     if (s) return s;
     if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "upload [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
     const size_t b = count * 16;
-    struct { void *dst; const void *src; } m[] = {
-        {w->pos + offset, pos4}, {w->vel + offset, vel4}, {w->ori + offset, ori4}, {w->tum + offset, tum4},
-        {w->aux + offset, aux4}, {w->rcs + offset, rcs4}, {w->sig + offset, sig4}, {w->rnd + offset, rnd4}};
-    for (auto &e : m) {
-        if (e.src) RSC_CUDA(cudaMemcpyAsync(e.dst, e.src, b, cudaMemcpyHostToDevice, w->stream));
+    uint4 **arr[8];
+    attribute_arrays(w, arr);
+    const void *src[8] = {pos4, vel4, ori4, tum4, aux4, rcs4, sig4, rnd4};
+    for (int k = 0; k < 8; k++) {
+        if (src[k] == nullptr || count == 0) continue;
+        if (w->perm == nullptr) {
+            RSC_CUDA(cudaMemcpyAsync(*arr[k] + offset, src[k], b, cudaMemcpyHostToDevice, w->stream));
+        } else {
+            /* caller's order -> slots, through the idle second buffer */
+            RSC_CUDA(cudaMemcpyAsync(w->alt[0], src[k], b, cudaMemcpyHostToDevice, w->stream));
+            rsc::k_scatter16<<<grid_of(count, rsc::kSortThreads), rsc::kSortThreads, 0, w->stream>>>(
+                *arr[k], w->alt[0], w->inv, offset, count);
+            RSC_CUDA(cudaGetLastError());
+            w->launches++;
+        }
     }
     RSC_CUDA(cudaStreamSynchronize(w->stream));
     if (aux4 || sig4) w->sig_aux_stale = false;
+    if (pos4) w->sort_due = true;
+    return RSC_OK;
+}
+
+int rsc_set_sort_interval(rsc_worker *w, int steps) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (steps < 0) return fail(RSC_ERR_ARG, "sort interval %d", steps);
+    w->sort_interval = steps;
+    return RSC_OK;
+}
+
+int rsc_sort_count(rsc_worker *w, uint64_t *count) {
+    if (w == nullptr || count == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
+    *count = w->sorts;
     return RSC_OK;
 }
 
@@ -617,11 +800,21 @@ int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float 
         w->sig_aux_stale = false;
     }
     const size_t b = count * 16;
-    struct { void *dst; const void *src; } m[] = {
-        {pos4, w->pos + offset}, {vel4, w->vel + offset}, {ori4, w->ori + offset}, {tum4, w->tum + offset},
-        {aux4, w->aux + offset}, {rcs4, w->rcs + offset}, {sig4, w->sig + offset}, {rnd4, w->rnd + offset}};
-    for (auto &e : m) {
-        if (e.dst) RSC_CUDA(cudaMemcpyAsync(e.dst, e.src, b, cudaMemcpyDeviceToHost, w->stream));
+    uint4 **arr[8];
+    attribute_arrays(w, arr);
+    void *dst[8] = {pos4, vel4, ori4, tum4, aux4, rcs4, sig4, rnd4};
+    for (int k = 0; k < 8; k++) {
+        if (dst[k] == nullptr || count == 0) continue;
+        if (w->perm == nullptr) {
+            RSC_CUDA(cudaMemcpyAsync(dst[k], *arr[k] + offset, b, cudaMemcpyDeviceToHost, w->stream));
+        } else {
+            /* slots -> caller's order, through the idle second buffer */
+            rsc::k_gather16<<<grid_of(count, rsc::kSortThreads), rsc::kSortThreads, 0, w->stream>>>(
+                w->alt[0], *arr[k], w->inv, offset, count);
+            RSC_CUDA(cudaGetLastError());
+            w->launches++;
+            RSC_CUDA(cudaMemcpyAsync(dst[k], w->alt[0], b, cudaMemcpyDeviceToHost, w->stream));
+        }
     }
     RSC_CUDA(cudaStreamSynchronize(w->stream));
     return RSC_OK;
@@ -684,7 +877,8 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
     RSC_CUDA(cudaGetLastError());
     w->launches++;
     w->sig_aux_stale = true;
-    return RSC_OK;
+    w->since_sort++;
+    return maybe_sort(w, pop, sim_desc, w->stream);
 }
 
 int rsc_update_debris_rcs(rsc_worker *w, const rsc_population *pop, const float sim_desc[16]) {
@@ -1259,9 +1453,13 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
     if (s) return s;
     s = batch_join_workers(b);
     if (s) return s;
+    const size_t n = b->w.size();
+    for (size_t i = 0; i < n; i++) {
+        s = maybe_sort(b->w[i], &b->pops[i], b->h_steps[i].sim, b->stream);
+        if (s) return s;
+    }
     s = batch_prepare(b, b->h_steps);
     if (s) return s;
-    const size_t n = b->w.size();
     /* LES slots this run reads: wait for their pending refills */
     std::vector<char> used(2 * n, 0);
     for (size_t r = 0; r < (size_t)steps * n; r++) used[2 * (r % n) + (b->h_steps[r].les_id & 1)] = 1;
@@ -1294,6 +1492,7 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
     RSC_CUDA(cudaEventRecord(b->ev_done, b->stream));
     for (size_t i = 0; i < n; i++) {
         rsc_worker *x = b->w[i];
+        x->since_sort += (uint64_t)steps;
         RSC_CUDA(cudaStreamWaitEvent(x->stream, b->ev_done, 0));
         memcpy(x->last_sim, sim_descs + ((size_t)(steps - 1) * n + i) * 16, sizeof(x->last_sim));
         x->have_pulse_desc = true;

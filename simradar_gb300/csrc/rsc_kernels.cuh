@@ -332,6 +332,7 @@ struct PulseArgs {
     unsigned rw_n;       /* range weight table length; <= 4 is kept in rwv */
     float rwv[4];
     int dense;
+    int coherent_span;   /* warp-coherent gate path when a warp spans fewer gates */
     int materialize;
     double *acc64;       /* G * 4 FP64 accumulators, zero between launches */
     unsigned *counter;

@@ -174,6 +174,45 @@ __host__ __device__ constexpr size_t pulse_warp_bytes(int mode, unsigned G) {
 }
 
 /* block blk of the nblk blocks that form one pulse */
+/* Largest number of gates a warp visits together on the coherent path; a
+ * wider spread goes through per-lane atomics. */
+/* The warp's candidate gates [w_lo, w_hi] over the lanes that have any; true
+ * when the span is at most `span` gates (the coherent path).  The host sets
+ * span to G when the state is in spatial order (neighbouring lanes share
+ * gates, and per-lane atomics would collide) and to 0 otherwise (random
+ * ranges: a warp spans most gates, and per-lane atomics rarely collide). */
+__device__ __forceinline__ bool warp_coherent(bool has, int k_lo, int k_hi, int span, int &w_lo, int &w_hi) {
+    if (span <= 0) return false;
+    const bool any = has && k_hi >= k_lo;
+    w_lo = (int)__reduce_min_sync(0xffffffffu, any ? (unsigned)k_lo : 0xffffffffu);
+    w_hi = (int)__reduce_max_sync(0xffffffffu, any ? (unsigned)k_hi : 0u);
+    if (w_lo == -1) {       /* no lane has a candidate */
+        w_hi = -2;
+        return true;
+    }
+    return w_hi - w_lo < span;
+}
+
+/* Add the warp's sum of four values into bin[0..3]: a transposed butterfly
+ * (6 shuffles instead of 20) leaves the sum of value c in lanes 8c..8c+7,
+ * and lanes 0, 8, 16, 24 add them to the warp's own bins (no other warp
+ * writes them, and one lane per address, so no atomic is needed). */
+__device__ __forceinline__ void warp_reduce4_add(float *bin, unsigned lane, float v0, float v1, float v2, float v3) {
+    const bool h16 = (lane & 16u) != 0;
+    float k0 = h16 ? v2 : v0, k1 = h16 ? v3 : v1;
+    const float s0 = h16 ? v0 : v2, s1 = h16 ? v1 : v3;
+    k0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
+    k1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+    const bool h8 = (lane & 8u) != 0;
+    float k = h8 ? k1 : k0;
+    const float s = h8 ? k0 : k1;
+    k = k + __shfl_xor_sync(0xffffffffu, s, 8);
+    k = k + __shfl_xor_sync(0xffffffffu, k, 4);
+    k = k + __shfl_xor_sync(0xffffffffu, k, 2);
+    k = k + __shfl_xor_sync(0xffffffffu, k, 1);
+    if ((lane & 7u) == 0u && k != 0.0f) bin[lane >> 3] += k;
+}
+
 template <int MODE>
 __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, unsigned nblk) {
     typedef PulseTraits<MODE> Tr;
@@ -261,6 +300,7 @@ __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, uns
                 k_hi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
             }
             const int maxc = min(kMaxCandidates, (int)__reduce_max_sync(0xffffffffu, (unsigned)max(k_hi - k_lo + 1, 0)));
+            int w_lo = 0, w_hi = -1;
             if constexpr (MODE == 2) {
                 for (int j = 0; j < maxc; j++) {
                     const int gate = k_lo + j;
@@ -272,6 +312,27 @@ __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, uns
                         nz = (w != 0.0);
                     }
                     bin_add<Acc>(wbins, 0xffffffffu, nz, gate, cw);
+                }
+            } else if (warp_coherent(in && finite, k_lo, k_hi, P.coherent_span, w_lo, w_hi)) {
+                /* the warp's candidates fall in a few gates (a state kept in
+                 * spatial order): visit them together and reduce each gate
+                 * across the warp, no atomics.  The gate origin is advanced
+                 * from w_lo by the reference's running-sum additions, so every
+                 * lane's origin is the same bit pattern as in the branch below */
+                float rkj = 0.0f;
+                if (MODE == 0) rkj = __ldg(P.rk + w_lo);
+                for (int gate = w_lo; gate <= w_hi; gate++) {
+                    float w = 0.0f;
+                    if (gate >= k_lo && gate <= k_hi) {
+                        if constexpr (MODE == 1) {
+                            w = weight_comp(P.rw, P.rwd, r - __ldg(P.rk + gate), r_lo - __ldg(P.rk_lo + gate));
+                        } else {
+                            w = range_weight_reg(P, r - rkj);
+                        }
+                    }
+                    warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, w * c.v[0], w * c.v[1], w * c.v[2],
+                                     w * c.v[3]);
+                    rkj = rkj + P.rdelta;
                 }
             } else {
                 /* plain: one gate origin is loaded and advanced by the same

@@ -104,6 +104,8 @@ def load_library():
         "rsc_get_stream": ([P, ctypes.POINTER(P)], I),
         "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
         "rsc_autotune": ([P, _f32p, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "rsc_set_sort_interval": ([P, I], I),
+        "rsc_sort_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
         "rsc_batch_create": ([ctypes.POINTER(P), I, ctypes.POINTER(P)], I),
         "rsc_batch_free": ([P], I),
         "rsc_batch_set_populations": ([P, ctypes.POINTER(Population)], I),
@@ -316,6 +318,17 @@ class Worker:
         s = ctypes.c_void_p()
         _check(self._lib.rsc_get_stream(self._h, ctypes.byref(s)))
         return s.value or 0
+
+    def set_sort_interval(self, steps):
+        """Steps between re-sorts of the background range into spatial
+        order (0: keep the caller's order)."""
+        _check(self._lib.rsc_set_sort_interval(self._h, int(steps)))
+
+    @property
+    def sort_count(self):
+        n = ctypes.c_uint64(0)
+        _check(self._lib.rsc_sort_count(self._h, ctypes.byref(n)))
+        return n.value
 
     def autotune(self, sim_desc):
         """Pick the pulse kernel's launch shape by timing (warps, blocks/SM)."""
