@@ -540,6 +540,7 @@ static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float
     if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
     if (uvwt4 == nullptr || desc == nullptr || nx == 0 || ny == 0 || nz == 0) return fail(RSC_ERR_ARG, "LES table");
     const size_t nn = (size_t)nx * ny * nz;
+    if (nn >= (1ull << 31)) return fail(RSC_ERR_UNSUPPORTED, "LES of %zu texels (the kernels index below 2^31)", nn);
     if (w->les_uvwt[0] != nullptr && (nx != w->les_nx || ny != w->les_ny || nz != w->les_nz)) {
         /* new dimensions: reallocate both slots (rs.c:3000-3016 releases them) */
         cudaStreamSynchronize(w->stream);
@@ -583,6 +584,7 @@ static int set_table2d(rsc_worker *w, Table2D *t, const float *a4, const float *
     if (a4 == nullptr || b4 == nullptr || desc == nullptr || nx == 0 || ny == 0) return fail(RSC_ERR_ARG, "2-D table");
     cudaStreamSynchronize(w->stream);
     const size_t nn = (size_t)nx * ny;
+    if (nn >= (1ull << 31)) return fail(RSC_ERR_UNSUPPORTED, "2-D table of %zu texels (the kernels index below 2^31)", nn);
     int s = upload_float4(&t->a, a4, nn);
     if (s) return s;
     s = upload_float4(&t->b, b4, nn);

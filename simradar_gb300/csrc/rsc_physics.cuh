@@ -110,13 +110,14 @@ __device__ __forceinline__ float4 read_image3d(const Image &im, float u, float v
     tex_axis(u, im.nx, &i0, &i1, &a);
     tex_axis(v, im.ny, &j0, &j1, &b);
     tex_axis(w, im.nz, &k0, &k1, &c);
-    const size_t sy = (size_t)im.nx, sz = (size_t)im.nx * (size_t)im.ny;
+    /* texel indices in 32 bits: the host keeps a volume below 2^31 texels */
+    const unsigned sy = (unsigned)im.nx, sz = (unsigned)im.nx * (unsigned)im.ny;
     const float4 *d = im.data;
-    const size_t r00 = j0 * sy + k0 * sz, r10 = j1 * sy + k0 * sz, r01 = j0 * sy + k1 * sz, r11 = j1 * sy + k1 * sz;
-    float4 t000 = ldg4(d + r00 + i0), t100 = ldg4(d + r00 + i1);
-    float4 t010 = ldg4(d + r10 + i0), t110 = ldg4(d + r10 + i1);
-    float4 t001 = ldg4(d + r01 + i0), t101 = ldg4(d + r01 + i1);
-    float4 t011 = ldg4(d + r11 + i0), t111 = ldg4(d + r11 + i1);
+    const unsigned r00 = j0 * sy + k0 * sz, r10 = j1 * sy + k0 * sz, r01 = j0 * sy + k1 * sz, r11 = j1 * sy + k1 * sz;
+    float4 t000 = ldg4(d + (r00 + i0)), t100 = ldg4(d + (r00 + i1));
+    float4 t010 = ldg4(d + (r10 + i0)), t110 = ldg4(d + (r10 + i1));
+    float4 t001 = ldg4(d + (r01 + i0)), t101 = ldg4(d + (r01 + i1));
+    float4 t011 = ldg4(d + (r11 + i0)), t111 = ldg4(d + (r11 + i1));
     float ma = 1.0f - a, mb = 1.0f - b, mc = 1.0f - c;
     float w000 = ma * mb * mc, w100 = a * mb * mc, w010 = ma * b * mc, w110 = a * b * mc;
     float w001 = ma * mb * c, w101 = a * mb * c, w011 = ma * b * c, w111 = a * b * c;
@@ -133,10 +134,11 @@ __device__ __forceinline__ float4 read_image2d(const Image &im, float u, float v
     float a, b;
     tex_axis(u, im.nx, &i0, &i1, &a);
     tex_axis(v, im.ny, &j0, &j1, &b);
-    const size_t sy = (size_t)im.nx;
+    const unsigned sy = (unsigned)im.nx;
     const float4 *d = im.data;
-    float4 t00 = ldg4(d + i0 + j0 * sy), t10 = ldg4(d + i1 + j0 * sy);
-    float4 t01 = ldg4(d + i0 + j1 * sy), t11 = ldg4(d + i1 + j1 * sy);
+    const unsigned r0 = j0 * sy, r1 = j1 * sy;
+    float4 t00 = ldg4(d + (r0 + i0)), t10 = ldg4(d + (r0 + i1));
+    float4 t01 = ldg4(d + (r1 + i0)), t11 = ldg4(d + (r1 + i1));
     float ma = 1.0f - a, mb = 1.0f - b;
     float w00 = ma * mb, w10 = a * mb, w01 = ma * b, w11 = a * b;
 #define RSC_BIL(L) (w00 * t00.L + w10 * t10.L + w01 * t01.L + w11 * t11.L)

@@ -13,7 +13,8 @@
  * GPU and the oracle even on the stretched LES grid, where log1p feeds the
  * wind lookup every pulse.
  *
- * Methods (all textbook mathematics, coefficients from the Taylor series):
+ * Methods (textbook mathematics; coefficients from the Taylor series or from
+ * least-squares fits made for this file, as noted):
  *   - sin/cos: Cody-Waite reduction by pi/2 split in three floats, applied
  *     with fmaf (the first step is exact for |x| < 2^22 * pi/2), then the
  *     Taylor polynomials of sin (to x^9) and cos (to x^10) on [-pi/4, pi/4].
@@ -25,10 +26,12 @@
  *     outside, log(u) + e / u with u = 1 + x rounded and e = (1 + x) - u
  *     formed exactly (the correction is below an ulp, so 1/u comes from the
  *     exponent and one Newton step, again without a division).
- *   - asin/acos: Taylor series of asin to s^21 on |s| <= 1/2 and the
- *     half-angle identity acos(x) = 2 asin(sqrt((1-x)/2)) above.
+ *   - asin/acos: asin(s) = s + s^3 P(s^2) on |s| <= 1/2, P a degree-4
+ *     least-squares fit made for this file (0.62 ulp in exact arithmetic),
+ *     and the half-angle identity acos(x) = 2 asin(sqrt((1-x)/2)) above.
  *   - atan/atan2: reduction to [0, 1], then to |u| <= tan(pi/8) by
- *     atan(t) = pi/4 + atan((t-1)/(t+1)), Taylor series to u^19.
+ *     atan(t) = pi/4 + atan((t-1)/(t+1)), atan(u) = u + u^3 Q(u^2) with Q a
+ *     degree-5 least-squares fit made for this file (0.59 ulp).
  *   - exp: k = rint(x/ln2), r = x - k ln2 (two-part), Taylor to r^7, 2^k by
  *     exponent construction.  pow(b, e) = exp(e log b) with the rounding error
  *     of the product carried by fmaf.
@@ -211,43 +214,44 @@ RSM_FN float rsm_logf(float x) {
 
 /* log(1 + x) */
 RSM_FN float rsm_log1pf(float x) {
-    if (rsm_isnan(x)) {
-        return x;
-    }
     if (x > -0x1.2bec34p-2f && x < 0x1.a8279ap-2f) {
         /* 1 + x in [sqrt(1/2), sqrt(2)): the polynomial on x directly,
          * without rounding 1 + x */
         return rsm_log1p_core(x);
     }
-    float u = 1.0f + x;
-    if (u == INFINITY || !(u > 0.0f)) {
+    const float u = 1.0f + x;
+    if (rsm_isnan(x) || !(u > 0.0f) || u == INFINITY) {
         return rsm_logf(u);
     }
-    /* log(1 + x) = log(u) + log(1 + e / u), e = (1 + x) - u exactly (u - 1 is
-     * exact here); e / u < 2^-24, so log(1 + e / u) = e / u to far below an
-     * ulp and 1 / u needs only a few correct bits: 2^-k (1.5 - m / 2) for
-     * u = m 2^k, m in [1, 2), refined once by Newton's step. */
-    float e = x - (u - 1.0f);
-    uint32_t b = rsm_f2u(u);
-    float m = rsm_u2f((b & 0x007fffffu) | 0x3f800000u);
-    float y = 1.5f - 0.5f * m;
-    y = y * (2.0f - m * y);
-    float inv = y * rsm_u2f((uint32_t)(254 - (int)((b >> 23) & 0xff)) << 23);
-    return rsm_logf(u) + e * inv;
+    /* u = m 2^k is normal here (u >= 2^-24).  log(1 + x) = log(u) +
+     * log(1 + e / u) with e = (1 + x) - u, exact (u - 1 is exact below 2^24,
+     * and above it e / u is far below an ulp of the result); e / u < 2^-24,
+     * so log(1 + e / u) = e / u and 1 / u needs only a few correct bits:
+     * 2^-k (1.5 - m / 2) for m in [1, 2), refined once by Newton's step.  The
+     * correction joins the polynomial's small part before the k ln 2 head. */
+    const float e = x - (u - 1.0f);
+    const uint32_t b = rsm_f2u(u);
+    int k = (int)(b >> 23) - 127;
+    const float m1 = rsm_u2f((b & 0x007fffffu) | 0x3f800000u);
+    float y = 1.5f - 0.5f * m1;
+    y = y * (2.0f - m1 * y);
+    const float inv = y * rsm_u2f((uint32_t)(127 - k) << 23);
+    float m = m1;
+    if (m > RSM_SQRT2) {
+        m = m * 0.5f;                         /* exact */
+        k += 1;
+    }
+    const float fk = (float)k;
+    return fk * RSM_LN2_HI + fmaf(fk, RSM_LN2_LO, rsm_log1p_core(m - 1.0f) + e * inv);
 }
 
-/* asin on |s| <= 1/2 : s + s z P(z), z = s^2 (Taylor series to s^21) */
+/* asin on |s| <= 1/2 : s + s z P(z), z = s^2, P the degree-4 fit */
 RSM_FN float rsm_asin_core(float s, float z) {
-    float p = 0x1.12ef3cp-7f;                 /* c10 =  46189/5505024 */
-    p = fmaf(p, z, 0x1.3fde50p-7f);               /* c9  =  12155/1245184 */
-    p = fmaf(p, z, 0x1.7a8788p-7f);               /* c8  =   6435/557056  */
-    p = fmaf(p, z, 0x1.c9999ap-7f);               /* c7  =    143/10240   */
-    p = fmaf(p, z, 0x1.1c4ec4p-6f);               /* c6  =    231/13312   */
-    p = fmaf(p, z, 0x1.6e8ba2p-6f);               /* c5  =     63/2816    */
-    p = fmaf(p, z, 0x1.f1c71cp-6f);               /* c4  =     35/1152    */
-    p = fmaf(p, z, 0x1.6db6dcp-5f);               /* c3  =      5/112     */
-    p = fmaf(p, z, 0x1.333334p-4f);               /* c2  =      3/40      */
-    p = fmaf(p, z, 0x1.555556p-3f);               /* c1  =      1/6       */
+    float p = 0x1.5625d6p-5f;
+    p = fmaf(p, z, 0x1.8ff98cp-6f);
+    p = fmaf(p, z, 0x1.741a60p-5f);
+    p = fmaf(p, z, 0x1.330612p-4f);
+    p = fmaf(p, z, 0x1.5555bap-3f);
     return fmaf(s * z, p, s);
 }
 
@@ -280,18 +284,15 @@ RSM_FN float rsm_acosf(float x) {
     return RSM_PI_HI - (a - RSM_PI_LO);
 }
 
-/* atan on |u| <= tan(pi/8) : u + u z Q(z), Taylor series to u^19 */
+/* atan on |u| <= tan(pi/8) : u + u z Q(z), Q the degree-5 fit */
 RSM_FN float rsm_atan_core(float u) {
     float z = u * u;
-    float q = -0x1.af286cp-5f;                /* -1/19 */
-    q = fmaf(q, z, 0x1.e1e1e2p-5f);               /*  1/17 */
-    q = fmaf(q, z, (-0x1.111112p-4f));            /* -1/15 */
-    q = fmaf(q, z, 0x1.3b13b2p-4f);               /*  1/13 */
-    q = fmaf(q, z, (-0x1.745d18p-4f));            /* -1/11 */
-    q = fmaf(q, z, 0x1.c71c72p-4f);               /*  1/9  */
-    q = fmaf(q, z, (-0x1.24924ap-3f));            /* -1/7  */
-    q = fmaf(q, z, 0x1.99999ap-3f);               /*  1/5  */
-    q = fmaf(q, z, (-0x1.555556p-2f));            /* -1/3  */
+    float q = 0x1.889eccp-5f;
+    q = fmaf(q, z, -0x1.5c2c30p-4f);
+    q = fmaf(q, z, 0x1.c49292p-4f);
+    q = fmaf(q, z, -0x1.2480d4p-3f);
+    q = fmaf(q, z, 0x1.99992cp-3f);
+    q = fmaf(q, z, -0x1.555554p-2f);
     return fmaf(u * z, q, u);
 }
 

@@ -9,7 +9,10 @@ the oracle: the reference-order pulse, the exact and FP64 sums with their
 absolute sums, and the state after the last step.
 
 The fixture pins the oracle and the GPU against regressions; it is made by
-the oracle, not by the reference (whose OpenCL path does not run here).
+the oracle, not by the reference (whose OpenCL path does not run here).  A
+deliberate change of the shared elementary functions (rsmath.h) changes the
+state bits on both sides at once; the fixture is then made again with this
+script.
 
     python tests/golden/make_golden.py
 """
