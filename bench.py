@@ -30,7 +30,8 @@ Extra sections on one GPU (added to the same JSON line):
              to back one after another.
   large      33,554,432 rain + 131,072 debris, LES 352x352x160, RHI
              0.5-20 deg at 0.02 deg, compensated form, I/Q streamed to pinned
-             host buffers every 100 pulses, one LES slot refilled on the copy
+             host buffers every 100 pulses and on to a .iq file by the
+             backend's background writer, one LES slot refilled on the copy
              stream during the run.
 """
 import argparse
@@ -415,6 +416,10 @@ def bench_batch(torch, rsc, synth, dev, steps):
 
 # ---------------------------------------------------------------------- large
 def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
+    import shutil
+    import tempfile
+
+    from simradar_gb300 import iqfile
     n_rain = 33554432
     cfg = synth.LESConfig(nx=352, ny=352, nz=160)
     debris = [(synth.OBJ_LEAF, 43691), (synth.OBJ_WOODBOARD_2X4, 43691), (synth.OBJ_BRICK, 43690)]
@@ -435,7 +440,15 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     B.set_precision(rsc.PULSE_COMPENSATED)
     ring = [torch.empty((chunk, 1, B.max_gates, 4), dtype=torch.float32).pin_memory() for _ in range(2)]
     stream = torch.cuda.ExternalStream(B.stream)
-    iq = np.zeros((chunks * chunk, GATES, 4), np.float32)
+    tmpdir = tempfile.mkdtemp(prefix="simradar_iq_")
+    iq_path = os.path.join(tmpdir, "large.iq")
+    params = {"c": 3.0e8, "prt": float(S.prt), "lambda": float(S.lam), "tx_power_watt": 50.0e3,
+              "antenna_gain_dbi": 44.5, "antenna_bw_deg": 1.0, "tau": 0.2e-6, "range_start": float(S.range_start),
+              "range_end": float(S.range_start + S.range_delta * (GATES - 1)), "range_delta": float(S.range_delta),
+              "elevation_start_deg": 0.5, "elevation_end_deg": 20.0, "elevation_delta_deg": 0.02,
+              "prf": 1.0 / float(S.prt), "dr": float(S.dr), "range_count": GATES}
+    writer = iqfile.IQWriter(iq_path, params, counts=S.counts, scan_mode="RHI", scan_start=0.5, scan_end=20.0,
+                             scan_delta=0.02, seed=777)
 
     def sims(k0):
         a = np.zeros((chunk, 1, 16), np.float32)
@@ -446,6 +459,11 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     def les_ids(slot):
         return np.full((chunk, 1), slot, np.int32)
 
+    def beam(k0):
+        el = np.array([S.scan[(k0 + j) % len(S.scan)][1] for j in range(chunk)], np.float32)
+        az = np.array([S.scan[(k0 + j) % len(S.scan)][0] for j in range(chunk)], np.float32)
+        return (np.arange(k0, k0 + chunk, dtype=np.float32) * np.float32(S.prt)), el, az
+
     B.autotune(sims(0)[0])
     B.run(sims(0), les_ids(0), out=ring[0].numpy())     # warm-up and graph capture
     B.synchronize()
@@ -455,11 +473,18 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     swap_at = chunks // 2
+
+    def drain(r):
+        ev, c = done[r]
+        ev.synchronize()
+        t, el, az = beam(chunk * (c + 1))
+        writer.write(ring[r].numpy()[:, 0], times=t, el_deg=el, az_deg=az, gain=float(S.gain))
+        done[r] = None
+
     for c in range(chunks):
         r = c % 2
         if done[r] is not None:
-            done[r][0].synchronize()
-            iq[done[r][1] * chunk:(done[r][1] + 1) * chunk] = ring[r].numpy()[:, 0, :GATES]
+            drain(r)
         slot = 1 if c >= swap_at else 0
         B.run(sims(chunk * (c + 1)), les_ids(slot), out=ring[r].numpy(), wait=False)
         ev = torch.cuda.Event()
@@ -469,23 +494,29 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
             # refill slot 1 while this chunk runs on slot 0
             B.set_les_async(0, 1, pin_u.numpy(), pin_c.numpy())
     e1.record(stream)
-    for r in range(2):
+    for r in (chunks % 2, (chunks + 1) % 2):
         if done[r] is not None:
-            done[r][0].synchronize()
-            iq[done[r][1] * chunk:(done[r][1] + 1) * chunk] = ring[r].numpy()[:, 0, :GATES]
+            drain(r)
     B.synchronize()
+    writer.flush()
     wall = time.perf_counter() - t0
     dev_ms = e0.elapsed_time(e1)
+    writer.close()
     pulses = chunks * chunk
+    d = iqfile.read_iq(iq_path)
+    shutil.rmtree(tmpdir, ignore_errors=True)
     B.close()
     W.close()
+    iq = d["iq"]
     return {"workload": "33,554,432 rain + 131,072 debris (leaf / 2x4 board / brick), LES 352x352x160, RHI 0.5-20 "
                         "deg / 0.02 deg, %d gates, compensated form; %d pulses in chunks of %d streamed to pinned "
-                        "host buffers, LES slot 1 refilled (2 x %d MB) on the copy stream during chunk %d"
-                        % (GATES, pulses, chunk, int(nxt.uvwt.nbytes / 1e6), swap_at - 1),
+                        "host buffers and on to a .iq file (background writer), LES slot 1 refilled (2 x %d MB) on "
+                        "the copy stream during chunk %d" % (GATES, pulses, chunk, int(nxt.uvwt.nbytes / 1e6),
+                                                               swap_at - 1),
             "pulses_per_s": pulses / wall, "device_pulses_per_s": pulses / (dev_ms / 1e3),
             "scatterer_updates_per_s": pulses / wall * nscat, "pulses": pulses,
-            "iq_finite": bool(np.isfinite(iq).all()), "iq_nonzero_pulses": int((np.abs(iq).sum(axis=(1, 2)) > 0).sum())}
+            "iq_file_pulses": int(iq.shape[0]), "iq_finite": bool(np.isfinite(iq).all()),
+            "iq_nonzero_pulses": int((np.abs(iq).sum(axis=(1, 2)) > 0).sum())}
 
 
 def run_ours(args, rank, world):

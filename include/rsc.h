@@ -253,6 +253,39 @@ int rsc_batch_get_stream(rsc_batch *b, void **stream);
 /* The pulse shape chosen by rsc_batch_autotune (0, 0 before it runs). */
 int rsc_batch_get_shape(rsc_batch *b, int *warps, int *blocks_per_sm);
 
+/* ---- I/Q output file (additive) ----
+ * The .iq file of simradar (simradar.c:340-366, headers iq.h:20-41, reader
+ * matlab/simradariq.m), byte for byte: a 1024-byte file header, then per
+ * pulse a 32-byte header (time, elevation, azimuth) and range_count float4
+ * (Ih, Qh, Iv, Qv).  Writes go to a background thread, so a pulse loop that
+ * streams I/Q blocks (rsc_batch_run_async into pinned buffers) is not held
+ * by the file system.  The reference keeps every pulse in host memory and
+ * writes the file at the end of the run. */
+typedef struct {
+    /* RSParams, rs_types.h:56-93 */
+    float c, prt, loss, lambda, tx_power_watt, antenna_gain_dbi, antenna_bw_deg, tau;
+    float range_start, range_end, range_delta;
+    float azimuth_start_deg, azimuth_end_deg, azimuth_delta_deg;
+    float elevation_start_deg, elevation_end_deg, elevation_delta_deg;
+    float domain_pad_factor, body_per_cell, prf, va, fn, antenna_bw_rad, dr;
+    uint32_t range_count;
+} rsc_iq_params;
+typedef struct rsc_iq_writer rsc_iq_writer;
+
+int rsc_iq_open(const char *path, const rsc_iq_params *params, const uint32_t counts[RSC_MAX_TYPES],
+                const char *scan_mode, float scan_start, float scan_end, float scan_delta, uint32_t seed,
+                rsc_iq_writer **out);
+/* Append `count` pulses: pulses4 holds count rows of row_gates float4 (the
+ * first range_count of each row are written, times `gain`); times, el_deg
+ * and az_deg hold one value per pulse (NULL writes zeros).  The data are
+ * copied before the call returns. */
+int rsc_iq_write(rsc_iq_writer *w, uint32_t count, const float *times, const float *el_deg, const float *az_deg,
+                 const float *pulses4, uint32_t row_gates, float gain);
+/* Wait until every appended pulse is in the file. */
+int rsc_iq_flush(rsc_iq_writer *w);
+int rsc_iq_close(rsc_iq_writer *w);
+const char *rsc_iq_last_error(void);
+
 /* Limits of rsc_make_pulse_noalloc (its scratch is a fixed device array of
  * about 9 KB per GPU that loads this library). */
 #define RSC_NOALLOC_MAX_GATES 128
