@@ -182,6 +182,20 @@ int rsc_set_sort_interval(rsc_worker *w, int steps);
 /* Number of sorts the worker has made. */
 int rsc_sort_count(rsc_worker *w, uint64_t *count);
 
+/* ---- fused step (additive) ----
+ * With the fused step on, rsc_advance_time records the advance
+ * and the next rsc_make_pulse runs both in one kernel, one pass over the
+ * state (the pulse reads exactly what the advance writes).  Any other call
+ * that reads or changes the state or the tables (download, upload, table
+ * setters, debris RCS, synchronize, a second advance, the batch) first runs
+ * the recorded advance on its own, so every result is the one of the
+ * separate calls; launch errors of a recorded advance are reported by the
+ * call that runs it.  The FP64 precision mode never fuses.  Off by default:
+ * both halves are bound by instruction issue, not by the state's bytes, and
+ * on a GB300 the separate kernels (each at its own occupancy) are about 3%
+ * faster per step than the fused one (2 M scatterers, 40 gates). */
+int rsc_set_fused_step(rsc_worker *w, int enable);
+
 /* ---- launch-shape autotuning (additive) ----
  * Time the pulse kernel of this worker at each candidate shape (warps per
  * block 4 / 8 / 16 and 1-4 resident blocks per SM) on the current state and

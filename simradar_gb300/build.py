@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libsimradar_gb300.so")
 SOURCES = ["rsc.cu", "rsc_iq.cpp"]
-DEPS = ["rsc.cu", "rsc_iq.cpp", "rsc_batch.cuh", "rsc_sort.cuh", "rsc_pulse.cuh", "rsc_kernels.cuh", "rsc_physics.cuh", "rsmath.h"]
+DEPS = ["rsc.cu", "rsc_iq.cpp", "rsc_batch.cuh", "rsc_sort.cuh", "rsc_step.cuh", "rsc_pulse.cuh", "rsc_kernels.cuh", "rsc_physics.cuh", "rsmath.h"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 

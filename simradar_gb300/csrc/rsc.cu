@@ -109,7 +109,20 @@ struct rsc_worker {
     unsigned *sort_key = nullptr, *sort_order = nullptr, *sort_hist = nullptr, *sort_blocks = nullptr;
     uint4 *alt[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     uint64_t sorts = 0;
+    /* fused step: rsc_advance_time records the advance, and the next
+     * rsc_make_pulse runs it together with the pulse (k_step); any other call
+     * that reads or changes the state or the tables runs it alone first */
+    int fuse = 0;
+    bool pend = false;
+    AdvanceArgs pend_a;
+    unsigned pend_blocks = 0;
+    rsc_population pend_pop;
+    float pend_sim[16] = {0};
 };
+
+namespace {
+int flush_pending(rsc_worker *w);
+}
 
 namespace {
 
@@ -452,6 +465,7 @@ int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float 
         return fail(RSC_ERR_ARG, "range_start / range_delta not finite");
     }
     cudaStreamSynchronize(w->stream);
+    w->pend = false;
     free_arrays(w);
     const size_t numel = (num_scats + 63) / 64 * 64;
     const size_t b4 = numel * sizeof(float4);
@@ -494,6 +508,8 @@ int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float 
 int rsc_set_range_weight(rsc_worker *w, const float *table, uint32_t n, const float desc[4]) {
     int s = check_worker(w);
     if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
     if (table == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "range weight table");
     if (!(desc[2] >= 0.0f) || (uint32_t)desc[2] >= n) return fail(RSC_ERR_ARG, "range weight max index %g >= %u", desc[2], n);
     cudaStreamSynchronize(w->stream);
@@ -510,6 +526,8 @@ int rsc_set_range_weight(rsc_worker *w, const float *table, uint32_t n, const fl
 int rsc_set_angular_weight(rsc_worker *w, const float *table, uint32_t n, const float desc[4]) {
     int s = check_worker(w);
     if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
     if (table == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "angular weight table");
     if (!(desc[2] >= 0.0f) || (uint32_t)desc[2] >= n) return fail(RSC_ERR_ARG, "angular weight max index %g >= %u", desc[2], n);
     cudaStreamSynchronize(w->stream);
@@ -522,6 +540,8 @@ int rsc_set_angular_weight(rsc_worker *w, const float *table, uint32_t n, const 
 
 int rsc_set_rcs_ellipsoid(rsc_worker *w, const float *table4, uint32_t n, const float desc[4]) {
     int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (table4 == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "ellipsoid RCS table");
     if (!(desc[2] >= 0.0f) || (uint32_t)desc[2] >= n) return fail(RSC_ERR_ARG, "ellipsoid max index %g >= %u", desc[2], n);
@@ -536,6 +556,8 @@ int rsc_set_rcs_ellipsoid(rsc_worker *w, const float *table4, uint32_t n, const 
 static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny,
                         uint32_t nz, const float desc[16], bool async) {
     int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
     if (uvwt4 == nullptr || desc == nullptr || nx == 0 || ny == 0 || nz == 0) return fail(RSC_ERR_ARG, "LES table");
@@ -581,6 +603,8 @@ int rsc_set_les_async(rsc_worker *w, int slot, const float *uvwt4, const float *
 
 static int set_table2d(rsc_worker *w, Table2D *t, const float *a4, const float *b4, uint32_t nx, uint32_t ny,
                        const float desc[16]) {
+    int s0 = flush_pending(w);
+    if (s0) return s0;
     if (a4 == nullptr || b4 == nullptr || desc == nullptr || nx == 0 || ny == 0) return fail(RSC_ERR_ARG, "2-D table");
     cudaStreamSynchronize(w->stream);
     const size_t nn = (size_t)nx * ny;
@@ -613,6 +637,8 @@ int rsc_set_rcs(rsc_worker *w, int index, const float *real4, const float *imag4
 
 int rsc_set_dff(rsc_worker *w, int slot, const float *icdf, uint32_t n, const float desc[16]) {
     int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (slot < 0 || slot > 1 || icdf == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "DFF table");
     /* db_atts reads icdf[floor(clamp(r * sf + {0, 1}, 0, sf))] (rs.cl:799-805) */
@@ -745,9 +771,56 @@ static int maybe_sort(rsc_worker *w, const rsc_population *pop, const float *sim
     return sort_worker(w, pop, sim, st);
 }
 
+}  // extern "C"
+
+namespace {
+
+/* Run a recorded advance on its own (k_advance) and do its bookkeeping. */
+int flush_pending(rsc_worker *w) {
+    if (!w->pend) return RSC_OK;
+    w->pend = false;
+    if (w->pend_blocks) {
+        rsc::k_advance<<<w->pend_blocks, rsc::kAdvanceThreads, 0, w->stream>>>(w->pend_a);
+        RSC_CUDA(cudaGetLastError());
+        w->launches++;
+    }
+    w->since_sort++;
+    return maybe_sort(w, &w->pend_pop, w->pend_sim, w->stream);
+}
+
+/* Launch shape of the step kernel: 256 threads (the advance's blocks), the
+ * pulse bins of its 8 warps, as many resident blocks as fit (at most 8). */
+int step_shape(int mode, rsc_worker *w, int *grid, size_t *smem) {
+    *smem = (size_t)(rsc::kAdvanceThreads / 32) * rsc::pulse_warp_bytes(mode, w->G) + 2 * w->G * sizeof(float);
+    int per_sm = 1;
+    cudaError_t e = mode == RSC_PULSE_PLAIN
+                        ? kernel_occupancy(rsc::k_step<0>, rsc::kAdvanceThreads, *smem, &per_sm)
+                        : kernel_occupancy(rsc::k_step<1>, rsc::kAdvanceThreads, *smem, &per_sm);
+    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "step kernel configuration: %s", cudaGetErrorString(e));
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 8) per_sm = 8;
+    *grid = w->num_sms * per_sm;
+    return RSC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsc_set_fused_step(rsc_worker *w, int enable) {
+    int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
+    w->fuse = enable ? 1 : 0;
+    return RSC_OK;
+}
+
 int rsc_upload(rsc_worker *w, size_t offset, size_t count, const float *pos4, const float *vel4, const float *ori4,
                const float *tum4, const float *aux4, const float *rcs4, const float *sig4, const uint32_t *rnd4) {
     int s = check_alloc(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "upload [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
     const size_t b = count * 16;
@@ -790,6 +863,8 @@ int rsc_sort_count(rsc_worker *w, uint64_t *count) {
 int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float *vel4, float *ori4, float *tum4,
                  float *aux4, float *rcs4, float *sig4, uint32_t *rnd4) {
     int s = check_alloc(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "download [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
     if ((aux4 || sig4) && w->sig_aux_stale && w->have_pulse_desc) {
@@ -870,11 +945,23 @@ static int fill_advance_args(rsc_worker *w, const rsc_population *pop, int les_i
 int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const float sim_desc[16]) {
     int s = check_alloc(w);
     if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
     AdvanceArgs a;
     unsigned blocks = 0;
     s = fill_advance_args(w, pop, les_id, sim_desc, a, &blocks);
     if (s) return s;
     if (blocks == 0) return RSC_OK;
+    if (w->fuse && w->precision != RSC_PULSE_F64) {
+        /* run with the next pulse, or alone by the next call that needs it */
+        w->pend = true;
+        w->pend_a = a;
+        w->pend_blocks = blocks;
+        w->pend_pop = *pop;
+        memcpy(w->pend_sim, sim_desc, sizeof(w->pend_sim));
+        w->sig_aux_stale = true;
+        return RSC_OK;
+    }
     rsc::k_advance<<<blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
     RSC_CUDA(cudaGetLastError());
     w->launches++;
@@ -885,6 +972,8 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
 
 int rsc_update_debris_rcs(rsc_worker *w, const rsc_population *pop, const float sim_desc[16]) {
     int s = check_alloc(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (pop == nullptr || sim_desc == nullptr) return fail(RSC_ERR_ARG, "population / sim_desc is NULL");
     AdvanceArgs a;
@@ -923,6 +1012,28 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     }
     const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
     P.materialize = mat ? 1 : 0;
+    if (w->pend && mode != RSC_PULSE_F64) {
+        /* the recorded advance and this pulse in one pass over the state */
+        int sgrid = 0;
+        size_t ssmem = 0;
+        s = step_shape(mode, w, &sgrid, &ssmem);
+        if (s) return s;
+        if (mode == RSC_PULSE_PLAIN) {
+            rsc::k_step<0><<<sgrid, rsc::kAdvanceThreads, ssmem, w->stream>>>(w->pend_a, P, w->pend_blocks);
+        } else {
+            rsc::k_step<1><<<sgrid, rsc::kAdvanceThreads, ssmem, w->stream>>>(w->pend_a, P, w->pend_blocks);
+        }
+        RSC_CUDA(cudaGetLastError());
+        w->pend = false;
+        w->launches++;
+        memcpy(w->last_sim, sim_desc, sizeof(w->last_sim));
+        w->have_pulse_desc = true;
+        w->sig_aux_stale = !mat;
+        w->since_sort++;
+        return maybe_sort(w, &w->pend_pop, w->pend_sim, w->stream);
+    }
+    s = flush_pending(w);
+    if (s) return s;
     launch_pulse(mode, P, grid, threads, smem, w->stream);
     RSC_CUDA(cudaGetLastError());
     w->launches++;
@@ -944,6 +1055,8 @@ int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain) {
 
 int rsc_synchronize(rsc_worker *w) {
     int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     RSC_CUDA(cudaStreamSynchronize(w->stream));
     return RSC_OK;
@@ -1238,6 +1351,8 @@ int batch_fill_steps(rsc_batch *b, int steps, const float *sim_descs, const int 
 /* Order the batch stream after every worker's queued work. */
 int batch_join_workers(rsc_batch *b) {
     for (rsc_worker *x : b->w) {
+        int s = flush_pending(x);
+        if (s) return s;
         RSC_CUDA(cudaEventRecord(b->ev_join, x->stream));
         RSC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     }
@@ -1250,6 +1365,8 @@ extern "C" {
 
 int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *blocks_per_sm_out) {
     int s = check_alloc(w);
+    if (s) return s;
+    s = flush_pending(w);
     if (s) return s;
     if (sim_desc == nullptr) return fail(RSC_ERR_ARG, "sim_desc is NULL");
     if (w->range_weight == nullptr || w->angular_weight == nullptr) {

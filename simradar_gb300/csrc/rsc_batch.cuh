@@ -15,7 +15,7 @@
 #ifndef SIMRADAR_GB300_RSC_BATCH_CUH
 #define SIMRADAR_GB300_RSC_BATCH_CUH
 
-#include "rsc_pulse.cuh"
+#include "rsc_step.cuh"
 
 namespace rsc {
 

@@ -46,7 +46,7 @@ struct AdvanceArgs {
 };
 
 /* ---- el_atts (rs.cl:653-739) ---- */
-__device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i) {
+__device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const float dt = sd[11];
     const uint32_t concept = __float_as_uint(sd[5]);
@@ -70,6 +70,8 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i) {
         a.pos[i] = pos;
         a.vel[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
         a.rnd[i] = seed;
+        po = pos;
+        xk = false;
         return;
     }
     float4 bg_vel = compute_bg_vel(pos, a.uvwt, a.wind, sd);
@@ -101,10 +103,13 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i) {
     a.pos[i] = pos;
     a.vel[i] = vel;
     a.rcs[i] = rcs;
+    po = pos;
+    xo = rcs;
+    xk = true;
 }
 
 /* ---- bg_atts (rs.cl:533-580) ---- */
-__device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i) {
+__device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const float dt = sd[11];
     float4 pos = a.pos[i];
@@ -122,6 +127,8 @@ __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i) {
         a.pos[i] = pos;
         a.vel[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
         a.rnd[i] = seed;
+        po = pos;
+        xk = false;
         return;
     }
     vel = compute_bg_vel(pos, a.uvwt, a.wind, sd);
@@ -129,10 +136,13 @@ __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i) {
     a.pos[i] = pos;
     a.vel[i] = vel;
     a.rcs[i] = rcs;
+    po = pos;
+    xo = rcs;
+    xk = true;
 }
 
 /* ---- fp_atts (rs.cl:590-648) ---- */
-__device__ __forceinline__ void rain_fp(const AdvanceArgs &a, size_t i) {
+__device__ __forceinline__ void rain_fp(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const float wav_num = sd[4];
     const float dt = sd[11];
@@ -159,10 +169,13 @@ __device__ __forceinline__ void rain_fp(const AdvanceArgs &a, size_t i) {
     vel.z = uv.z;
     a.vel[i] = vel;
     a.rcs[i] = rcs;
+    po = pos;
+    xo = rcs;
+    xk = true;
 }
 
 /* ---- db_atts (rs.cl:744-907) ---- */
-__device__ __forceinline__ void debris_step(const AdvanceArgs &a, const DebrisType &T, size_t i) {
+__device__ __forceinline__ void debris_step(const AdvanceArgs &a, const DebrisType &T, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const uint32_t concept = __float_as_uint(sd[5]);
     const float dt = sd[11];
@@ -231,6 +244,9 @@ __device__ __forceinline__ void debris_step(const AdvanceArgs &a, const DebrisTy
         a.tum[i] = f4(0.0f, 0.0f, 0.0f, 1.0f);
         a.rcs[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
         a.rnd[i] = seed;
+        po = pos;
+        xo = f4(0.0f, 0.0f, 0.0f, 0.0f);
+        xk = true;
         return;
     }
     float4 vel_bg = compute_bg_vel(pos, a.uvwt, a.wind, sd);
@@ -261,6 +277,9 @@ __device__ __forceinline__ void debris_step(const AdvanceArgs &a, const DebrisTy
     a.vel[i] = vel;
     a.tum[i] = tum;
     a.rcs[i] = rcs;
+    po = pos;
+    xo = rcs;
+    xk = true;
 }
 
 __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned long long j) {
@@ -274,25 +293,42 @@ __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned lon
 
 /* block b of one time step: blocks [0, rain_blocks) take the background
  * range, the rest the concatenated debris ranges */
-__device__ __forceinline__ void advance_body(const AdvanceArgs &a, unsigned b) {
+/* One scatterer of block b of a time step (blocks [0, rain_blocks) take the
+ * background, the rest the debris types in order): advanced in memory, and
+ * its new position and backscatter returned for a pulse formed in the same
+ * pass.  False when the thread has no scatterer. */
+__device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, unsigned long long &i_out, float4 &pos,
+                                            float4 &rcs) {
+    bool known = true;
     if (b < a.rain_blocks) {
         unsigned long long j = (unsigned long long)b * kAdvanceThreads + threadIdx.x;
-        if (j >= a.rain_count) return;
+        if (j >= a.rain_count) return false;
         size_t i = (size_t)(a.rain_origin + j);
         if (a.rain_mode == 1) {
-            rain_el(a, i);
+            rain_el(a, i, pos, rcs, known);
         } else if (a.rain_mode == 0) {
-            rain_bg(a, i);
+            rain_bg(a, i, pos, rcs, known);
         } else {
-            rain_fp(a, i);
+            rain_fp(a, i, pos, rcs, known);
         }
-        return;
+        if (!known) rcs = a.rcs[i];   /* respawned: the stored backscatter stays */
+        i_out = i;
+        return true;
     }
     unsigned long long j = (unsigned long long)(b - a.rain_blocks) * kAdvanceThreads + threadIdx.x;
-    if (a.ntypes == 0 || j >= a.deb_prefix[a.ntypes]) return;
+    if (a.ntypes == 0 || j >= a.deb_prefix[a.ntypes]) return false;
     int t = debris_type_of(a, j);
     const DebrisType &T = a.types[t];
-    debris_step(a, T, (size_t)(T.origin + (j - a.deb_prefix[t])));
+    size_t i = (size_t)(T.origin + (j - a.deb_prefix[t]));
+    debris_step(a, T, i, pos, rcs, known);
+    i_out = i;
+    return true;
+}
+
+__device__ __forceinline__ void advance_body(const AdvanceArgs &a, unsigned b) {
+    unsigned long long i;
+    float4 pos, rcs;
+    (void)advance_one(a, b, i, pos, rcs);
 }
 
 /* 5 blocks of 256 per SM (<= 51 registers): the step is a chain of dependent

@@ -213,45 +213,49 @@ __device__ __forceinline__ void warp_reduce4_add(float *bin, unsigned lane, floa
     if ((lane & 7u) == 0u && k != 0.0f) bin[lane >> 3] += k;
 }
 
+/* One block's share of a pulse: per-warp bins in shared memory, filled one
+ * scatterer per lane (add), then summed over the block into the grid's FP64
+ * accumulator, the last block converting (finish).  Used by the pulse kernel
+ * (scatterers loaded from memory) and by the fused step kernel (scatterers
+ * just advanced, in registers). */
 template <int MODE>
-__device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, unsigned nblk) {
+struct PulseBins {
     typedef PulseTraits<MODE> Tr;
     typedef typename Tr::Acc Acc;
     typedef typename Acc::bin_t bin_t;
-    constexpr unsigned kMain = Tr::kMain;                /* bin_t per gate in the main bins */
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned G = P.G;
-    const unsigned words = G * kMain;
-    const unsigned nwarps = blockDim.x >> 5;
-    const unsigned warp = threadIdx.x >> 5;
-    const unsigned lane = threadIdx.x & 31u;
-    bin_t *bins = reinterpret_cast<bin_t *>(smem_raw);
-    float *mini_all = reinterpret_cast<float *>(bins + (size_t)nwarps * words);   /* compensated: FP32 mini bins */
-    for (unsigned t = threadIdx.x; t < nwarps * words; t += blockDim.x) bins[t] = (bin_t)0;
-    if (MODE == 1) {
-        for (unsigned t = threadIdx.x; t < nwarps * G * kBinStride32; t += blockDim.x) mini_all[t] = 0.0f;
-    }
-    __syncthreads();
-    bin_t *wbins = bins + (size_t)warp * words;
-    float *mini = mini_all + (size_t)warp * G * kBinStride32;
-    float *fbins = (MODE == 1) ? mini : reinterpret_cast<float *>(wbins);   /* where FP32 atomics go */
+    static constexpr unsigned kMain = Tr::kMain;   /* bin_t per gate in the main bins */
+    bin_t *bins, *wbins;
+    float *mini, *fbins;
+    unsigned G, words, nwarps, warp, lane;
 
-    const unsigned long long stride = (unsigned long long)nblk * blockDim.x;
-    const unsigned long long n = P.n;
-    /* every lane of a warp runs the same number of iterations so the warp
-     * collectives below see the full warp */
-    const unsigned long long base0 = (unsigned long long)blk * blockDim.x + (threadIdx.x & ~31u);
-    for (unsigned long long base = base0; base < n; base += stride) {
-        const unsigned long long i = base + lane;
-        const bool in = i < n;
+    __device__ __forceinline__ void init(const PulseArgs &P) {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        G = P.G;
+        words = G * kMain;
+        nwarps = blockDim.x >> 5;
+        warp = threadIdx.x >> 5;
+        lane = threadIdx.x & 31u;
+        bins = reinterpret_cast<bin_t *>(smem_raw);
+        float *mini_all = reinterpret_cast<float *>(bins + (size_t)nwarps * words);   /* compensated: FP32 mini bins */
+        for (unsigned t = threadIdx.x; t < nwarps * words; t += blockDim.x) bins[t] = (bin_t)0;
+        if (MODE == 1) {
+            for (unsigned t = threadIdx.x; t < nwarps * G * kBinStride32; t += blockDim.x) mini_all[t] = 0.0f;
+        }
+        __syncthreads();
+        wbins = bins + (size_t)warp * words;
+        mini = mini_all + (size_t)warp * G * kBinStride32;
+        fbins = (MODE == 1) ? mini : reinterpret_cast<float *>(wbins);   /* where FP32 atomics go */
+    }
+
+    /* Scatterer i (position p, backscatter x) of this lane, if `in`.  Every
+     * lane of the warp calls it together (warp collectives inside). */
+    __device__ __forceinline__ void add(const PulseArgs &P, bool in, unsigned long long i, float4 p, float4 x) {
         Acc c;
         c.set(0, 0, 0, 0);
         float r = 0.0f, r_lo = 0.0f;
         double r64 = 0.0;
         bool finite = false;
         if (in) {
-            float4 p = __ldg(P.pos + i);
-            float4 x = __ldg(P.rcs + i);
             if constexpr (MODE == 2) {
                 double px = p.x, py = p.y, pz = p.z;
                 r64 = sqrt(px * px + py * py + pz * pz);
@@ -420,53 +424,77 @@ __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, uns
             __syncwarp();
         }
     }
-    __syncthreads();
 
-    /* block sum of each output (warp bins in warp order), added into the
-     * grid's FP64 accumulator with one global atomic per output: no block
-     * waits on another, and FP64 carries the FP32 and double-float block sums
-     * exactly enough that the order of the atomics does not show */
-    const unsigned outs = G * 4;
-    for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
-        const unsigned k = o >> 2, l = o & 3u;
-        double v;
-        if constexpr (Acc::kWords == 2) {
-            float hi = 0.0f, lo = 0.0f;
-            for (unsigned wv = 0; wv < nwarps; wv++) {
-                const float *b = reinterpret_cast<const float *>(bins) + (size_t)wv * words + k * 8;
-                float s, e;
-                two_sum(hi, b[l], s, e);
-                hi = s;
-                lo = lo + (e + b[4 + l]);
+    __device__ __forceinline__ void finish(const PulseArgs &P, unsigned nblk) {
+        __syncthreads();
+        /* block sum of each output (warp bins in warp order), added into the
+         * grid's FP64 accumulator with one global atomic per output: no block
+         * waits on another, and FP64 carries the FP32 and double-float block sums
+         * exactly enough that the order of the atomics does not show */
+        const unsigned outs = G * 4;
+        for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
+            const unsigned k = o >> 2, l = o & 3u;
+            double v;
+            if constexpr (Acc::kWords == 2) {
+                float hi = 0.0f, lo = 0.0f;
+                for (unsigned wv = 0; wv < nwarps; wv++) {
+                    const float *b = reinterpret_cast<const float *>(bins) + (size_t)wv * words + k * 8;
+                    float s, e;
+                    two_sum(hi, b[l], s, e);
+                    hi = s;
+                    lo = lo + (e + b[4 + l]);
+                }
+                v = (double)hi + (double)lo;
+            } else {
+                bin_t acc = (bin_t)0;
+                for (unsigned wv = 0; wv < nwarps; wv++) acc = acc + bins[(size_t)wv * words + k * kMain + l];
+                v = (double)acc;
             }
-            v = (double)hi + (double)lo;
-        } else {
-            bin_t acc = (bin_t)0;
-            for (unsigned wv = 0; wv < nwarps; wv++) acc = acc + bins[(size_t)wv * words + k * kMain + l];
-            v = (double)acc;
+            if (v != 0.0) atomicAdd(P.acc64 + o, v);
         }
-        if (v != 0.0) atomicAdd(P.acc64 + o, v);
+        __threadfence();
+        __syncthreads();
+        __shared__ bool s_last;
+        if (threadIdx.x == 0) {
+            unsigned ticket = atomicAdd(P.counter, 1u);
+            s_last = (ticket == nblk - 1);
+        }
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        /* last block: every other block's atomics are visible (each fenced
+         * before taking its ticket); convert, and leave the accumulator and the
+         * counter at zero for the next launch */
+        for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
+            const double v = __ldcg(P.acc64 + o);
+            reinterpret_cast<float *>(P.pulse)[o] = (float)v;
+            if (MODE == 2) P.pulse64[o] = v;
+            P.acc64[o] = 0.0;
+        }
+        if (threadIdx.x == 0) *P.counter = 0u;
     }
-    __threadfence();
-    __syncthreads();
-    __shared__ bool s_last;
-    if (threadIdx.x == 0) {
-        unsigned ticket = atomicAdd(P.counter, 1u);
-        s_last = (ticket == nblk - 1);
+};
+
+template <int MODE>
+__device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, unsigned nblk) {
+    PulseBins<MODE> B;
+    B.init(P);
+    const unsigned long long stride = (unsigned long long)nblk * blockDim.x;
+    const unsigned long long n = P.n;
+    /* every lane of a warp runs the same number of iterations so the warp
+     * collectives see the full warp */
+    const unsigned long long base0 = (unsigned long long)blk * blockDim.x + (threadIdx.x & ~31u);
+    for (unsigned long long base = base0; base < n; base += stride) {
+        const unsigned long long i = base + B.lane;
+        const bool in = i < n;
+        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), x = p;
+        if (in) {
+            p = __ldg(P.pos + i);
+            x = __ldg(P.rcs + i);
+        }
+        B.add(P, in, i, p, x);
     }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    /* last block: every other block's atomics are visible (each fenced
-     * before taking its ticket); convert, and leave the accumulator and the
-     * counter at zero for the next launch */
-    for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
-        const double v = __ldcg(P.acc64 + o);
-        reinterpret_cast<float *>(P.pulse)[o] = (float)v;
-        if (MODE == 2) P.pulse64[o] = v;
-        P.acc64[o] = 0.0;
-    }
-    if (threadIdx.x == 0) *P.counter = 0u;
+    B.finish(P, nblk);
 }
 
 template <int MODE>

@@ -105,6 +105,7 @@ def load_library():
         "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
         "rsc_autotune": ([P, _f32p, ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "rsc_set_sort_interval": ([P, I], I),
+        "rsc_set_fused_step": ([P, I], I),
         "rsc_sort_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
         "rsc_batch_create": ([ctypes.POINTER(P), I, ctypes.POINTER(P)], I),
         "rsc_batch_free": ([P], I),
@@ -323,6 +324,10 @@ class Worker:
         """Steps between re-sorts of the background range into spatial
         order (0: keep the caller's order)."""
         _check(self._lib.rsc_set_sort_interval(self._h, int(steps)))
+
+    def set_fused_step(self, enable):
+        """Run advance_time with the following make_pulse in one kernel."""
+        _check(self._lib.rsc_set_fused_step(self._h, 1 if enable else 0))
 
     @property
     def sort_count(self):

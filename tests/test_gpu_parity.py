@@ -283,3 +283,41 @@ def test_errors_are_status_codes(backend):
     with pytest.raises(backend.BackendError):
         W.upload(99, pos=np.zeros((5, 4), np.float32))  # beyond the arrays
     W.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fused_step_matches_separate(backend, oracle_lib, scene_db, precision):
+    """advance_time followed by make_pulse in one kernel (set_fused_step) gives
+    the state of the separate kernels bit for bit and the same pulses within
+    the summation bound; the oracle agrees."""
+    O = oracle_lib
+    S = scene_db
+    pop = synth.population(S)
+    Wf, Ws = backend.Worker(0), backend.Worker(0)
+    for W in (Wf, Ws):
+        synth.load_worker(W, S)
+        W.set_precision(precision)
+    Wf.set_fused_step(True)
+    Ws.set_fused_step(False)
+    st = O.OracleState(S.state)
+    for k in range(5):
+        sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+        Wf.make_pulse(sd)
+        Ws.make_pulse(sd)
+        gf, gs = Wf.download_pulse(1.0), Ws.download_pulse(1.0)
+        direct, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+        if precision == 0:
+            assert_pulse_close(gf, direct, ab, "fused pulse %d" % k)
+            assert_pulse_close(gs, direct, ab, "separate pulse %d" % k)
+        else:
+            r64, ab64 = O.make_pulse_f64(st, S, sd, return_abs=True)
+            assert_comp_close(gf, r64, ab64, "fused compensated pulse %d" % k)
+        Wf.advance_time(pop, 0, sd)
+        Ws.advance_time(pop, 0, sd)
+        O.advance_time(st, S, S.counts, S.les[0], sd)
+    a, b = Wf.download(STATE_FIELDS), Ws.download(STATE_FIELDS)
+    for f in STATE_FIELDS:
+        assert np.array_equal(bits(a[f]), bits(b[f])), f
+    assert_state_equal(a, st.s, where="fused ")
+    Wf.close()
+    Ws.close()
