@@ -157,6 +157,13 @@ int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain);
 /* Wait for all work queued on the worker (clFinish). */
 int rsc_synchronize(rsc_worker *w);
 
+/* The latest pulse copied to pulse4 (range_count float4, no gain) in the
+ * worker's stream order, without waiting: the copy is complete after
+ * rsc_synchronize.  With page-locked pulse4 the host can queue the next
+ * pulses while earlier copies are in flight (additive; the reference reads
+ * each pulse with a blocking clEnqueueReadBuffer, rs.c:5115). */
+int rsc_download_pulse_async(rsc_worker *w, float *pulse4);
+
 /* Pulse-formation precision, RSC_PULSE_* (additive, default PLAIN). */
 int rsc_set_pulse_precision(rsc_worker *w, int mode);
 

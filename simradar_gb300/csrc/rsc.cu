@@ -1053,6 +1053,14 @@ int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain) {
     return RSC_OK;
 }
 
+int rsc_download_pulse_async(rsc_worker *w, float *pulse4) {
+    int s = check_alloc(w);
+    if (s) return s;
+    if (pulse4 == nullptr) return fail(RSC_ERR_ARG, "pulse4 is NULL");
+    RSC_CUDA(cudaMemcpyAsync(pulse4, w->pulse, w->G * sizeof(float4), cudaMemcpyDeviceToHost, w->stream));
+    return RSC_OK;
+}
+
 int rsc_synchronize(rsc_worker *w) {
     int s = check_worker(w);
     if (s) return s;

@@ -98,6 +98,7 @@ def load_library():
         "rsc_make_pulse": ([P, _f32p], I),
         "rsc_download_pulse": ([P, _f32p, F], I),
         "rsc_synchronize": ([P], I),
+        "rsc_download_pulse_async": ([P, _f32p], I),
         "rsc_set_pulse_precision": ([P, I], I),
         "rsc_set_materialize_sig_aux": ([P, I], I),
         "rsc_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
@@ -298,6 +299,13 @@ class Worker:
             out = np.empty((self.range_count, 4), dtype=np.float32)
         _check(self._lib.rsc_download_pulse(self._h, _fp(out), float(gain)))
         return out
+
+    def download_pulse_async(self, out):
+        """Queue the copy of the latest pulse (no gain) into `out`, a
+        (range_count, 4) float32 array (page-locked for an asynchronous
+        copy); it is complete after synchronize()."""
+        assert out.shape == (self.range_count, 4)
+        _check(self._lib.rsc_download_pulse_async(self._h, _fp(out)))
 
     def synchronize(self):
         _check(self._lib.rsc_synchronize(self._h))

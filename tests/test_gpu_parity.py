@@ -321,3 +321,25 @@ def test_fused_step_matches_separate(backend, oracle_lib, scene_db, precision):
     assert_state_equal(a, st.s, where="fused ")
     Wf.close()
     Ws.close()
+
+
+def test_download_pulse_async(backend, scene_db):
+    """The queued copy holds the same pulse as the blocking read (which
+    applies the gain), for pulses queued back to back between advances."""
+    S = scene_db
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    pop = synth.population(S)
+    outs = np.zeros((3, S.range_count, 4), np.float32)
+    refs = []
+    for k in range(3):
+        sd = synth.pulse_sim_desc(S, k)
+        W.make_pulse(sd)
+        W.download_pulse_async(outs[k])
+        W.synchronize()
+        refs.append(W.download_pulse(2.0))
+        W.advance_time(pop, 0, sd)
+    for k in range(3):
+        assert np.any(outs[k] != 0.0)
+        assert np.array_equal(outs[k] * np.float32(2.0), refs[k]), k
+    W.close()
