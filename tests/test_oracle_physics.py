@@ -174,3 +174,159 @@ def test_wind_lookup_against_float64(oracle_lib):
     d = np.abs(st.s["vel"] - ref)
     assert np.all(d <= 1e-5 * np.abs(ref).max() + 1e-6), "wind: max diff %g" % d.max()
     assert math.isfinite(float(d.max()))
+
+
+# ---------------------------------------------------------------- debris
+def qmul(l, r):
+    """quat_mult (rs.cl:54-60), (x, y, z, w) rows."""
+    lx, ly, lz, lw = l.T
+    rx, ry, rz, rw = r.T
+    return np.stack([lw * rx - lz * ry + ly * rz + lx * rw,
+                     lw * ry + lz * rx + ly * rw - lx * rz,
+                     lw * rz + lz * rw - ly * rx + lx * ry,
+                     lw * rw - lz * rz - ly * ry - lx * rx], axis=1)
+
+
+def qconj(q):
+    return q * np.array([-1.0, -1.0, -1.0, 1.0])
+
+
+def qrot(v, q):
+    return qmul(qmul(q, v), qconj(q))
+
+
+def normalize4(v):
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def read_image2d64(img, u, v):
+    ny, nx = img.shape[:2]
+    out = np.zeros((u.shape[0], 4))
+    idx, wts = [], []
+    for c, n in ((u, nx), (v, ny)):
+        t = c - 0.5
+        i0 = np.floor(t)
+        a = t - i0
+        i0 = i0.astype(np.int64)
+        idx.append((np.clip(i0, 0, n - 1), np.clip(i0 + 1, 0, n - 1)))
+        wts.append((1.0 - a, a))
+    im = img.astype(np.float64)
+    for dx in (0, 1):
+        for dy in (0, 1):
+            out += (wts[0][dx] * wts[1][dy])[:, None] * im[idx[1][dy], idx[0][dx]]
+    return out
+
+
+def debris_rcs64(pos, ori, re, im, rd, cross_pol):
+    """compute_debris_rcs (rs.cl:282-359)."""
+    el = np.arctan2(pos[:, 2], np.hypot(pos[:, 0], pos[:, 1]))
+    az = np.arctan2(pos[:, 0], pos[:, 1])
+    se, ce = np.sin(0.5 * (el + np.pi / 2)), np.cos(0.5 * (el + np.pi / 2))
+    sa, ca = np.sin(0.5 * az), np.cos(0.5 * az)
+    oc = (np.stack([-se, ce, se, ce], axis=1) * ca[:, None] + np.stack([ce, se, ce, -se], axis=1) * sa[:, None]) \
+        * math.sqrt(0.5)
+    R = qmul(ori, oc)
+    q = np.stack([R[:, 0], R[:, 2], -R[:, 1], R[:, 3]], axis=1)
+    qx, qy, qz, qw = q.T
+    barg = qw * qw + qz * qz - qy * qy - qx * qx
+    lump = (barg > 0.999847) | (barg < -0.999847)
+    alpha = np.where(lump, 0.0, np.arctan2(qy * qz - qw * qx, qx * qz + qw * qy))
+    beta = np.where(lump, 0.0, np.arccos(np.clip(barg, -1, 1)))
+    gamma = np.where(lump, np.sign(qz) * np.arccos(np.clip(qw, -1, 1)) * 2.0,
+                     np.arctan2(qy * qz + qw * qx, qw * qy - qx * qz))
+    u = alpha * rd[0] + rd[4]
+    v = beta * rd[1] + rd[5]
+    r_, i_ = read_image2d64(re, u, v), read_image2d64(im, u, v)
+    cg, sg = np.cos(gamma), np.sin(gamma)
+    hh_r = cg * (cg * r_[:, 0] - r_[:, 2] * sg) - sg * (cg * r_[:, 2] - r_[:, 1] * sg)
+    hh_i = cg * (cg * i_[:, 0] - i_[:, 2] * sg) - sg * (cg * i_[:, 2] - i_[:, 1] * sg)
+    vv_r = cg * (cg * r_[:, 1] + r_[:, 2] * sg) + sg * (cg * r_[:, 2] + r_[:, 0] * sg)
+    vv_i = cg * (cg * i_[:, 1] + i_[:, 2] * sg) + sg * (cg * i_[:, 2] + i_[:, 0] * sg)
+    ss = np.stack([hh_r, hh_i, vv_r, vv_i], axis=1)
+    if cross_pol:
+        hv_r = cg * (cg * r_[:, 2] + r_[:, 0] * sg) - sg * (cg * r_[:, 1] + r_[:, 2] * sg)
+        hv_i = cg * (cg * i_[:, 2] + i_[:, 0] * sg) - sg * (cg * i_[:, 1] + i_[:, 2] * sg)
+        vh_r = cg * (cg * r_[:, 2] - r_[:, 1] * sg) + sg * (cg * r_[:, 0] - r_[:, 2] * sg)
+        vh_i = cg * (cg * i_[:, 2] - i_[:, 1] * sg) + sg * (cg * i_[:, 0] - i_[:, 2] * sg)
+        ss = ss + np.stack([vh_r, vh_i, hv_r, hv_i], axis=1)
+    near = np.abs(np.abs(barg) - 0.999847) < 1e-5
+    return ss, near
+
+
+@pytest.mark.parametrize("concept", [synth.CONCEPT_DBU, synth.CONCEPT_DBU | synth.CONCEPT_CROSS_POL])
+def test_debris_step_against_float64(oracle_lib, concept):
+    """db_atts (rs.cl:744-907) for scatterers that are not respawned: the
+    attitude update, the ADM force and torque (compute_dudt_dwdt
+    rs.cl:195-261), the bounded velocity, the tumble and the debris RCS,
+    against float64; lookups at the oracle's FP32 position and attitude."""
+    O = oracle_lib
+    S = synth.make_scene(num_rain=16, debris=[(synth.OBJ_LEAF, 3000), (synth.OBJ_BRICK, 3000)], les_count=1,
+                         concept=concept, seed=11)
+    rng = np.random.default_rng(8)
+    n = S.num_scats
+    S.state["vel"][:, :3] = rng.uniform(-15.0, 15.0, (n, 3)).astype(np.float32)
+    q = rng.standard_normal((n, 4))
+    S.state["ori"][:] = (q / np.linalg.norm(q, axis=1, keepdims=True)).astype(np.float32)
+    t = np.concatenate([rng.normal(0, 0.02, (n, 3)), np.ones((n, 1))], axis=1)
+    S.state["tum"][:] = (t / np.linalg.norm(t, axis=1, keepdims=True)).astype(np.float32)
+    sd = synth.pulse_sim_desc(S, 5)
+    st = O.OracleState(S.state)
+    O.advance_time(st, S, S.counts, S.les[0], sd)
+    dt = float(sd[11])
+    cross = bool(concept & synth.CONCEPT_CROSS_POL)
+    origin = S.counts[0]
+    for t_i, cnt in enumerate(S.counts[1:]):
+        sl = slice(origin, origin + cnt)
+        origin += cnt
+        cd_img, cm_img, ad = S.adm[t_i]
+        re, im, rd = S.rcs_tables[t_i]
+        pos0 = S.state["pos"][sl].astype(np.float64)
+        vel0 = S.state["vel"][sl].astype(np.float64)
+        ori_in = S.state["ori"][sl].astype(np.float64)
+        tum_in = S.state["tum"][sl].astype(np.float64)
+        ori = normalize4(qmul(ori_in, tum_in))
+        p = pos0.copy()
+        p[:, :3] += vel0[:, :3] * dt
+        out = outside64(p, sd) | near_face(p, sd, 1e-3)
+        P32, O32 = st.s["pos"][sl].astype(np.float64), st.s["ori"][sl].astype(np.float64)
+        assert np.allclose(O32[~out], ori[~out], rtol=0, atol=2e-6)
+        assert np.allclose(P32[~out], p[~out], rtol=1e-6, atol=1e-4)
+        bg = read_image3d64(S.les[0].uvwt, wind_index64(P32, S.les_desc, sd))
+        ur = bg - vel0
+        uh = qrot(normalize4(ur), qconj(O32))
+        beta = np.arccos(np.clip(uh[:, 0], -1, 1))
+        alpha = np.arctan2(uh[:, 2], uh[:, 1])
+        neg = alpha < 0
+        alpha = np.where(neg, np.pi + alpha, alpha)
+        beta = np.where(neg, -beta, beta)
+        cd = read_image2d64(cd_img, beta * ad[0] + ad[4], alpha * ad[1] + ad[5])
+        cm = read_image2d64(cm_img, beta * ad[0] + ad[4], alpha * ad[1] + ad[5])
+        Ta = float(ad[15])
+        u2 = np.sum(ur[:, :3] ** 2, axis=1)
+        dudt = Ta * u2[:, None] * qrot(cd, O32) + np.array([0.0, 0.0, -9.8, 0.0])
+        inv = np.array([ad[12], ad[13], ad[14], 0.0], np.float64)
+        dwdt = np.radians(Ta * u2[:, None] * inv * cm)
+        vxy = vel0[:, :2] + dudt[:, :2] * dt
+        lhs, rhs = np.linalg.norm(vxy, axis=1), 3.0 * np.linalg.norm(bg[:, :2], axis=1)
+        bnd = lhs > rhs
+        vel = vel0 + dudt * np.array([dt, dt, dt, 0.0])
+        vel[bnd, :2] = bg[bnd, :2]
+        dw = dwdt * np.array([dt, dt, dt, 0.0])
+        c, s = np.cos(dw), np.sin(dw)
+        tum = normalize4(np.stack([c[:, 0] * s[:, 1] * s[:, 2] + s[:, 0] * c[:, 1] * c[:, 2],
+                                   c[:, 0] * s[:, 1] * c[:, 2] - s[:, 0] * c[:, 1] * s[:, 2],
+                                   c[:, 0] * c[:, 1] * s[:, 2] + s[:, 0] * s[:, 1] * c[:, 2],
+                                   c[:, 0] * c[:, 1] * c[:, 2] - s[:, 0] * s[:, 1] * s[:, 2]], axis=1))
+        rcs, near = debris_rcs64(P32, O32, re, im, rd, cross)
+        # leave out rounding-sized neighbourhoods of the branch decisions
+        ill = (np.abs(uh[:, 0]) > 0.9999) | (np.abs(np.arctan2(uh[:, 2], uh[:, 1])) < 1e-4) | \
+            (np.abs(lhs - rhs) < 1e-4 * (rhs + 1e-3)) | near
+        m = ~out & ~ill
+        assert m.sum() > 0.8 * cnt
+        V, T, X = st.s["vel"][sl][m], st.s["tum"][sl][m], st.s["rcs"][sl][m]
+        dv = np.abs(V - vel[m])
+        assert np.all(dv <= 1e-5 * np.abs(vel[m]) + 1e-4), "type %d velocity: max diff %g" % (t_i, dv.max())
+        assert np.all(np.abs(T - tum[m]) <= 1e-5), "type %d tumble: max diff %g" % (t_i, np.abs(T - tum[m]).max())
+        scale = np.abs(rcs[m]).max(axis=1, keepdims=True) + 1e-30
+        dx = np.abs(X - rcs[m]) / scale
+        assert np.all(dx <= 1e-3), "type %d rcs: max rel diff %g" % (t_i, dx.max())
