@@ -55,3 +55,44 @@ def test_cdll_signature(backend, sym):
     lib = backend.load_library()
     fn = getattr(lib, sym)
     assert fn.restype is ctypes.c_int
+
+
+def test_header_compiles_as_c_and_links(tmp_path, backend):
+    """rs.c is C: the header must compile with a C compiler (C99, all
+    warnings as errors) and a C program must link against the library and
+    get status codes back without a GPU (no device here is an error code,
+    not an exit)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "host.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <string.h>
+#include "rsc.h"
+int main(void) {
+    rsc_population pop;
+    rsc_iq_params iq;
+    int n = -1;
+    memset(&pop, 0, sizeof(pop));
+    memset(&iq, 0, sizeof(iq));
+    if (sizeof(iq) != 100) return 10;
+    if (rsc_worker_create(0, NULL) != RSC_ERR_ARG) return 11;
+    if (rsc_make_pulse(NULL, NULL) != RSC_ERR_ARG) return 12;
+    if (rsc_advance_time(NULL, &pop, 0, NULL) != RSC_ERR_ARG) return 13;
+    if (rsc_batch_run(NULL, 1, NULL, NULL, NULL, 0) != RSC_ERR_ARG) return 14;
+    (void)rsc_device_count(&n);
+    printf("%d %s\n", n, rsc_last_error());
+    return 0;
+}
+''')
+    exe = tmp_path / "host"
+    lib = backend.library_path()
+    cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+           str(src), "-o", str(exe), lib, "-Wl,-rpath," + os.path.dirname(lib)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
