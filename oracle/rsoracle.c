@@ -187,9 +187,13 @@ static inline of4 compute_ellipsoid_rcs(of4 pos, const of4 *table, const float *
     float fidx = cl_clamp(fmaf(pos.w, td[0], td[1]), 0.0f, td[2]);
     uint32_t idx = cl_f2u_rtz(fidx);
     of4 xz = table[idx];
-    float beta = rsm_atan2f(pos.z, sqrtf(pos.x * pos.x + pos.y * pos.y));
-    float cb = rsm_cosf(beta);
-    return f4(xz.x, xz.y, xz.x + (xz.z - xz.x) * cb * cb, xz.y + (xz.w - xz.y) * cb * cb);
+    /* cos^2 of the elevation beta = atan2(z, |xy|), formed as |xy|^2 / |xyz|^2:
+     * the same quantity as cos(beta) * cos(beta) without the two
+     * transcendental calls (1 at the origin, where atan2(0, 0) = 0) */
+    const float h2 = pos.x * pos.x + pos.y * pos.y;
+    const float r2 = h2 + pos.z * pos.z;
+    const float cb2 = r2 > 0.0f ? h2 / r2 : 1.0f;
+    return f4(xz.x, xz.y, xz.x + (xz.z - xz.x) * cb2, xz.y + (xz.w - xz.y) * cb2);
 }
 
 /* ---- compute_debris_rcs (rs.cl:282-359) ---- */

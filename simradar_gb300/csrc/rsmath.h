@@ -129,10 +129,11 @@ RSM_FN void rsm_sincos_reduced(float r, float q, float *s_out, float *c_out) {
     pc = fmaf(pc, z, 0x1.555556p-5f);            /*  1/24      */
     pc = fmaf(pc, z, (-0.5f));
     float cs = fmaf(z, pc, 1.0f);
-    /* quadrant from the low two bits of q (q is an integer-valued float):
-     * (sin, cos) of r + quad pi/2 = (sn, cs), (cs, -sn), (-sn, -cs), (-cs, sn) */
-    float q4 = q - 4.0f * floorf(q * 0.25f);
-    int quad = (int)q4;
+    /* quadrant from the low two bits of q (an integer-valued float, |q| <
+     * 2^23, so the conversion is exact; two's complement gives q mod 4 for
+     * negative q too): (sin, cos) of r + quad pi/2 = (sn, cs), (cs, -sn),
+     * (-sn, -cs), (-cs, sn) */
+    const int quad = (int)q & 3;
     const int swap = quad & 1;
     float s = swap ? cs : sn;
     float c = swap ? sn : cs;
