@@ -218,6 +218,31 @@ __device__ __forceinline__ void warp_reduce4_add(float *bin, unsigned lane, floa
  * accumulator, the last block converting (finish).  Used by the pulse kernel
  * (scatterers loaded from memory) and by the fused step kernel (scatterers
  * just advanced, in registers). */
+/* The same warp sum added into a double-float bin row (hi[0..3], lo[0..3])
+ * with an error-free addition: the compensated form's coherent path, which
+ * then needs no FP32 mini bins. */
+__device__ __forceinline__ void warp_reduce4_add_df(float *df, unsigned lane, float v0, float v1, float v2, float v3) {
+    const bool h16 = (lane & 16u) != 0;
+    float k0 = h16 ? v2 : v0, k1 = h16 ? v3 : v1;
+    const float s0 = h16 ? v0 : v2, s1 = h16 ? v1 : v3;
+    k0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
+    k1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+    const bool h8 = (lane & 8u) != 0;
+    float k = h8 ? k1 : k0;
+    const float s = h8 ? k0 : k1;
+    k = k + __shfl_xor_sync(0xffffffffu, s, 8);
+    k = k + __shfl_xor_sync(0xffffffffu, k, 4);
+    k = k + __shfl_xor_sync(0xffffffffu, k, 2);
+    k = k + __shfl_xor_sync(0xffffffffu, k, 1);
+    if ((lane & 7u) == 0u && k != 0.0f) {
+        const unsigned c = lane >> 3;
+        float hi, e;
+        two_sum(df[c], k, hi, e);
+        df[c] = hi;
+        df[4 + c] = df[4 + c] + e;
+    }
+}
+
 template <int MODE>
 struct PulseBins {
     typedef PulseTraits<MODE> Tr;
@@ -250,6 +275,7 @@ struct PulseBins {
     /* Scatterer i (position p, backscatter x) of this lane, if `in`.  Every
      * lane of the warp calls it together (warp collectives inside). */
     __device__ __forceinline__ void add(const PulseArgs &P, bool in, unsigned long long i, float4 p, float4 x) {
+        bool mini_used = false;   /* FP32 mini bins written this iteration (compensated form) */
         Acc c;
         c.set(0, 0, 0, 0);
         float r = 0.0f, r_lo = 0.0f;
@@ -305,6 +331,7 @@ struct PulseBins {
             }
             const int maxc = min(kMaxCandidates, (int)__reduce_max_sync(0xffffffffu, (unsigned)max(k_hi - k_lo + 1, 0)));
             int w_lo = 0, w_hi = -1;
+            bool coherent = false;
             if constexpr (MODE == 2) {
                 for (int j = 0; j < maxc; j++) {
                     const int gate = k_lo + j;
@@ -317,7 +344,7 @@ struct PulseBins {
                     }
                     bin_add<Acc>(wbins, 0xffffffffu, nz, gate, cw);
                 }
-            } else if (warp_coherent(in && finite, k_lo, k_hi, P.coherent_span, w_lo, w_hi)) {
+            } else if ((coherent = warp_coherent(in && finite, k_lo, k_hi, P.coherent_span, w_lo, w_hi))) {
                 /* the warp's candidates fall in a few gates (a state kept in
                  * spatial order): visit them together and reduce each gate
                  * across the warp, no atomics.  The gate origin is advanced
@@ -334,8 +361,13 @@ struct PulseBins {
                             w = range_weight_reg(P, r - rkj);
                         }
                     }
-                    warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, w * c.v[0], w * c.v[1], w * c.v[2],
-                                     w * c.v[3]);
+                    if constexpr (MODE == 1) {
+                        warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, w * c.v[0],
+                                            w * c.v[1], w * c.v[2], w * c.v[3]);
+                    } else {
+                        warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, w * c.v[0], w * c.v[1],
+                                         w * c.v[2], w * c.v[3]);
+                    }
                     rkj = rkj + P.rdelta;
                 }
             } else {
@@ -365,7 +397,9 @@ struct PulseBins {
                 }
             }
             /* a non-finite signal meets every gate (0 * inf = NaN in pass 1) */
+            mini_used = !coherent;
             if (__any_sync(0xffffffffu, in && !finite)) {
+                mini_used = true;
                 for (unsigned k = 0; k < G; k++) {
                     bool valid = in && !finite;
                     Acc cw;
@@ -406,7 +440,7 @@ struct PulseBins {
                 warp_sum_into<Acc>(wbins + (size_t)k * kMain, cw);
             }
         }
-        if constexpr (MODE == 1) {
+        if (MODE == 1 && mini_used) {
             /* fold the FP32 mini bins into the warp's double-float bins */
             __syncwarp();
             float *df = reinterpret_cast<float *>(wbins);
