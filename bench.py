@@ -505,6 +505,12 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     dev_ms = e0.elapsed_time(e1)
     writer.close()
     pulses = chunks * chunk
+    # RS_populate's initial state for the same population, made on the host
+    # and copied in overlapped blocks (what a session start costs)
+    pa = rsc.PopulateArgs.make(19760520, S.concept, S.box[:3], S.box[3:], S.counts, S.dsd_r, S.dsd_cdf)
+    t1 = time.perf_counter()
+    rsc.populate_upload(W, pa)
+    populate_s = time.perf_counter() - t1
     d = iqfile.read_iq(iq_path)
     shutil.rmtree(tmpdir, ignore_errors=True)
     B.close()
@@ -517,6 +523,7 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
                                                                swap_at - 1),
             "pulses_per_s": pulses / wall, "device_pulses_per_s": pulses / (dev_ms / 1e3),
             "scatterer_updates_per_s": pulses / wall * nscat, "pulses": pulses,
+            "populate_s": populate_s,
             "iq_file_pulses": int(iq.shape[0]), "iq_finite": bool(np.isfinite(iq).all()),
             "iq_nonzero_pulses": int((np.abs(iq).sum(axis=(1, 2)) > 0).sum())}
 

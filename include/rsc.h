@@ -274,6 +274,39 @@ int rsc_batch_get_stream(rsc_batch *b, void **stream);
 /* The pulse shape chosen by rsc_batch_autotune (0, 0 before it runs). */
 int rsc_batch_get_shape(rsc_batch *b, int *warps, int *blocks_per_sm);
 
+/* ---- initial state (additive) ----
+ * The scatterers RS_populate (rs.c:4568-4814) makes from RS_set_random_seed:
+ * the same draws of the C library's rand() in the same order (glibc's
+ * generator, reproduced, so the result does not depend on the host's libc),
+ * for one worker whose type ranges follow one another from slot 0, outside
+ * the fixed-position concept (whose anchor planes rs.c keeps making).  The
+ * "(float)rand() / RAND_MAX * size + origin" products are rounded before the
+ * sum (no fused multiply-add).  The ellipsoid table, the debris RCS refresh
+ * and the warm-up advance of RS_populate stay in rs.c. */
+typedef struct {
+    uint32_t seed;                       /* H->random_seed */
+    uint32_t concept;                    /* H->sim_concept bits */
+    float domain_origin[3], domain_size[3];   /* RS_get_domain */
+    uint32_t num_types;                  /* H->num_types (1 + debris types) */
+    uint64_t origins[RSC_MAX_TYPES], counts[RSC_MAX_TYPES];
+    const float *dsd_r, *dsd_cdf;        /* H->dsd_r / H->dsd_cdf, NULL when no DSD is set */
+    uint32_t dsd_count;                  /* H->dsd_count, 0 when no DSD is set */
+} rsc_populate_args;
+
+/* The first `count` values of rand() after srand(seed). */
+int rsc_rand_sequence(uint32_t seed, uint32_t count, int32_t *out);
+/* The whole initial state into host arrays of num_scats float4 / uint4
+ * (NULL skips vel, ori, tum, rcs); dsd_pop (dsd_count entries, may be NULL)
+ * counts the drops per bin as H->dsd_pop does. */
+int rsc_populate_host(const rsc_populate_args *a, size_t num_scats, float *pos4, float *vel4, float *ori4,
+                      float *tum4, float *aux4, float *rcs4, uint32_t *rnd4, uint32_t *dsd_pop);
+/* The same state made straight into an allocated worker: generated on the
+ * host in blocks that go to the device by page-locked asynchronous copies
+ * while the next block is generated (RS_populate + RS_upload without the
+ * full host arrays). */
+int rsc_populate_upload(rsc_worker *w, const rsc_populate_args *a, uint32_t *dsd_pop);
+const char *rsc_populate_last_error(void);
+
 /* ---- I/Q output file (additive) ----
  * The .iq file of simradar (simradar.c:340-366, headers iq.h:20-41, reader
  * matlab/simradariq.m), byte for byte: a 1024-byte file header, then per

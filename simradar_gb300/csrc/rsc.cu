@@ -18,6 +18,7 @@
 #include "../../include/rsc.h"
 #include "rsc_batch.cuh"
 #include "rsc_sort.cuh"
+#include "rsc_populate.h"
 
 using rsc::AdvanceArgs;
 using rsc::DebrisType;
@@ -806,6 +807,91 @@ int step_shape(int mode, rsc_worker *w, int *grid, size_t *smem) {
 }  // namespace
 
 extern "C" {
+
+}  // extern "C"
+
+namespace rsc {
+/* the constant part of RS_populate's state (rs.c:4672-4744): zero velocity,
+ * the attitude facing the beam, no tumbling, unit RCS, no signal; slots past
+ * the populated ones zero */
+__global__ void __launch_bounds__(256) k_fill_population(float4 *vel, float4 *ori, float4 *tum, float4 *rcs,
+                                                         float4 *sig, unsigned long long used,
+                                                         unsigned long long numel) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * 256 + threadIdx.x;
+    if (i >= numel) return;
+    const bool u = i < used;
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    vel[i] = z;
+    sig[i] = z;
+    ori[i] = u ? make_float4(0.5f, -0.5f, -0.5f, 0.5f) : z;
+    tum[i] = u ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : z;
+    rcs[i] = u ? make_float4(1.0f, 0.0f, 1.0f, 0.0f) : z;
+}
+}  // namespace rsc
+
+extern "C" {
+
+int rsc_populate_upload(rsc_worker *w, const rsc_populate_args *args, uint32_t *dsd_pop) {
+    int s = check_alloc(w);
+    if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
+    if (args == nullptr) return fail(RSC_ERR_ARG, "args is NULL");
+    rscpop::Generator g;
+    const char *why = "";
+    s = g.init(args, &why);
+    if (s) return fail(s, "%s", why);
+    if (g.total > w->num_scats) return fail(RSC_ERR_ARG, "the type ranges exceed the %zu scatterers", w->num_scats);
+    if (dsd_pop && args->dsd_count) memset(dsd_pop, 0, args->dsd_count * sizeof(uint32_t));
+    RSC_CUDA(cudaStreamSynchronize(w->stream));
+    free_sort(w);   /* the state is replaced: slots in the caller's order again */
+    const size_t chunk = (size_t)1 << 20;
+    float *hp[2] = {nullptr, nullptr}, *ha[2] = {nullptr, nullptr};
+    uint32_t *hr[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaSuccess;
+    for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+        e = cudaMallocHost((void **)&hp[b], chunk * 16);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&ha[b], chunk * 16);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&hr[b], chunk * 16);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming);
+    }
+    bool used[2] = {false, false};
+    for (size_t c = 0; e == cudaSuccess && c < g.total; c += chunk) {
+        const int b = (int)((c / chunk) & 1);
+        if (used[b]) e = cudaEventSynchronize(ev[b]);   /* the copies out of this buffer are done */
+        if (e != cudaSuccess) break;
+        const size_t n = g.total - c < chunk ? g.total - c : chunk;
+        g.fill(n, hp[b], ha[b], hr[b], dsd_pop);   /* overlaps the copies of the other buffer */
+        e = cudaMemcpyAsync(w->pos + c, hp[b], n * 16, cudaMemcpyHostToDevice, w->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(w->aux + c, ha[b], n * 16, cudaMemcpyHostToDevice, w->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(w->rnd + c, hr[b], n * 16, cudaMemcpyHostToDevice, w->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[b], w->stream);
+        used[b] = true;
+    }
+    const size_t tail = w->numel - g.total;
+    if (e == cudaSuccess && tail) e = cudaMemsetAsync(w->pos + g.total, 0, tail * 16, w->stream);
+    if (e == cudaSuccess && tail) e = cudaMemsetAsync(w->aux + g.total, 0, tail * 16, w->stream);
+    if (e == cudaSuccess && tail) e = cudaMemsetAsync(w->rnd + g.total, 0, tail * 16, w->stream);
+    if (e == cudaSuccess) {
+        rsc::k_fill_population<<<(unsigned)((w->numel + 255) / 256), 256, 0, w->stream>>>(
+            w->vel, w->ori, w->tum, w->rcs, w->sig, g.total, w->numel);
+        e = cudaGetLastError();
+        w->launches++;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+    for (int b = 0; b < 2; b++) {
+        if (hp[b]) cudaFreeHost(hp[b]);
+        if (ha[b]) cudaFreeHost(ha[b]);
+        if (hr[b]) cudaFreeHost(hr[b]);
+        if (ev[b]) cudaEventDestroy(ev[b]);
+    }
+    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "populate: %s", cudaGetErrorString(e));
+    w->sig_aux_stale = false;
+    w->have_pulse_desc = false;
+    w->sort_due = true;
+    return RSC_OK;
+}
 
 int rsc_set_fused_step(rsc_worker *w, int enable) {
     int s = check_worker(w);

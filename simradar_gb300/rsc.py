@@ -447,3 +447,75 @@ class Batch:
         s = ctypes.c_void_p()
         _check(self._lib.rsc_batch_get_stream(self._h, ctypes.byref(s)))
         return s.value or 0
+
+
+class PopulateArgs(ctypes.Structure):
+    """rsc_populate_args: what RS_populate reads from its handle."""
+    _fields_ = [("seed", ctypes.c_uint32), ("concept", ctypes.c_uint32),
+                ("domain_origin", ctypes.c_float * 3), ("domain_size", ctypes.c_float * 3),
+                ("num_types", ctypes.c_uint32),
+                ("origins", ctypes.c_uint64 * RSC_MAX_TYPES), ("counts", ctypes.c_uint64 * RSC_MAX_TYPES),
+                ("dsd_r", _f32p), ("dsd_cdf", _f32p), ("dsd_count", ctypes.c_uint32)]
+
+    @classmethod
+    def make(cls, seed, concept, origin, size, counts, dsd_r=None, dsd_cdf=None):
+        a = cls()
+        a.seed = int(seed) & 0xFFFFFFFF
+        a.concept = int(concept)
+        for k in range(3):
+            a.domain_origin[k] = float(origin[k])
+            a.domain_size[k] = float(size[k])
+        a.num_types = len(counts)
+        acc = 0
+        for k, c in enumerate(counts):
+            a.origins[k] = acc
+            a.counts[k] = int(c)
+            acc += int(c)
+        if dsd_r is not None:
+            a._keep = (f32(dsd_r), f32(dsd_cdf))
+            a.dsd_r, a.dsd_cdf = _fp(a._keep[0]), _fp(a._keep[1])
+            a.dsd_count = len(dsd_r)
+        return a
+
+
+def _pop_lib():
+    L = load_library()
+    L.rsc_rand_sequence.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)]
+    L.rsc_populate_host.argtypes = [ctypes.POINTER(PopulateArgs), ctypes.c_size_t] + [_f32p] * 6 + \
+        [_u32p, ctypes.POINTER(ctypes.c_uint32)]
+    L.rsc_populate_upload.argtypes = [ctypes.c_void_p, ctypes.POINTER(PopulateArgs), ctypes.POINTER(ctypes.c_uint32)]
+    L.rsc_populate_last_error.restype = ctypes.c_char_p
+    return L
+
+
+def rand_sequence(seed, count):
+    """The first `count` values of glibc's rand() after srand(seed)."""
+    L = _pop_lib()
+    out = np.zeros(count, dtype=np.int32)
+    st = L.rsc_rand_sequence(int(seed) & 0xFFFFFFFF, int(count), out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    if st != RSC_OK:
+        raise BackendError(st, L.rsc_populate_last_error().decode())
+    return out
+
+
+def populate_host(args, num_scats):
+    """RS_populate's initial state as host arrays (dict of (num_scats, 4))."""
+    L = _pop_lib()
+    arr = {f: np.zeros((num_scats, 4), np.float32) for f in ("pos", "vel", "ori", "tum", "aux", "rcs")}
+    arr["rnd"] = np.zeros((num_scats, 4), np.uint32)
+    pop = np.zeros(max(1, args.dsd_count), np.uint32)
+    st = L.rsc_populate_host(ctypes.byref(args), num_scats, _fp(arr["pos"]), _fp(arr["vel"]), _fp(arr["ori"]),
+                             _fp(arr["tum"]), _fp(arr["aux"]), _fp(arr["rcs"]), _up(arr["rnd"]),
+                             pop.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    if st != RSC_OK:
+        raise BackendError(st, L.rsc_populate_last_error().decode())
+    arr["sig"] = np.zeros((num_scats, 4), np.float32)
+    return arr, pop[:args.dsd_count]
+
+
+def populate_upload(worker, args):
+    """Generate the initial state straight into an allocated worker."""
+    L = _pop_lib()
+    pop = np.zeros(max(1, args.dsd_count), np.uint32)
+    _check(L.rsc_populate_upload(worker._h, ctypes.byref(args), pop.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+    return pop[:args.dsd_count]
