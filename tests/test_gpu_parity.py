@@ -397,3 +397,40 @@ def test_debris_only(backend, oracle_lib):
         O.advance_time(st, S, S.counts, S.les[0], sd)
         assert_state_equal(W.download(STATE_FIELDS), st.s, where="debris-only step %d " % k)
     W.close()
+
+
+@pytest.mark.parametrize("mode", [0.0, 1.0, 2.0])
+def test_debris_flux_field_respawn(backend, oracle_lib, mode):
+    """Concept C (debris flux from velocity, rs.cl:795-835): respawned debris
+    take their cell from the inverse-CDF table, placed plainly, on the
+    stretched grid (mode 1) or scaled to the domain (mode 2)."""
+    O = oracle_lib
+    S = synth.make_scene(num_rain=2000, debris=[(synth.OBJ_LEAF, 400), (synth.OBJ_BRICK, 400)], les_count=1,
+                         concept=synth.CONCEPT_DBU | synth.CONCEPT_DFF, seed=41)
+    push_to_edges(S, n_rain=100, n_deb=200)
+    icdf = np.linspace(0.0, 8.999, 2048).astype(np.float32)   # 3 x 3 cells
+    desc = np.zeros(16, np.float32)
+    desc[0] = desc[1] = np.float32(1.0 / 3.0)
+    desc[4] = desc[5] = 1.02
+    desc[8] = desc[9] = 2.0
+    desc[13] = 3.0
+    desc[14] = mode
+    desc[15] = 2047.0
+    S.dff, S.dff_desc = icdf, desc
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    for slot in (0, 1):
+        W.set_dff(slot, icdf, desc)
+    st = O.OracleState(S.state)
+    pop = synth.population(S)
+    for k in range(3):
+        sd = synth.pulse_sim_desc(S, k)
+        W.make_pulse(sd)
+        W.advance_time(pop, 0, sd)
+        O.advance_time(st, S, S.counts, S.les[0], sd)
+        assert_state_equal(W.download(STATE_FIELDS), st.s, where="DFF mode %g step %d " % (mode, k))
+    # debris respawned from the table sit at the minimum height
+    deb = slice(S.counts[0], S.num_scats)
+    moved = (st.s["rnd"][deb] != S.state["rnd"][deb]).any(axis=1)
+    assert moved.sum() >= 100
+    W.close()
