@@ -37,12 +37,25 @@ int fail(int code, const char *fmt, ...) {
     return code;
 }
 
+/* A failed CUDA call: the runtime also keeps the error as its "last error",
+ * which a later cudaGetLastError() after a good launch would report again;
+ * it is read (cleared) here.  An error that leaves the context unusable
+ * stays, as it must. */
+int cuda_fail(int code, const char *fmt, ...) {
+    (void)cudaGetLastError();
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
 #define RSC_CUDA(call)                                                                          \
     do {                                                                                        \
         cudaError_t e_ = (call);                                                                \
         if (e_ != cudaSuccess) {                                                                \
-            return fail(e_ == cudaErrorMemoryAllocation ? RSC_ERR_NOMEM : RSC_ERR_CUDA,         \
-                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return cuda_fail(e_ == cudaErrorMemoryAllocation ? RSC_ERR_NOMEM : RSC_ERR_CUDA,    \
+                             "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
         }                                                                                       \
     } while (0)
 
@@ -130,7 +143,7 @@ namespace {
 int check_worker(rsc_worker *w) {
     if (w == nullptr) return fail(RSC_ERR_ARG, "worker is NULL");
     cudaError_t e = cudaSetDevice(w->device);
-    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "cudaSetDevice(%d): %s", w->device, cudaGetErrorString(e));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_CUDA, "cudaSetDevice(%d): %s", w->device, cudaGetErrorString(e));
     return RSC_OK;
 }
 
@@ -315,7 +328,7 @@ int pulse_shape(int mode, bool batch, uint32_t G, int want_warps, int want_per_s
         e = batch ? kernel_occupancy(rsc::k_pulse_batch<2>, *threads, *smem, &per_sm)
                   : kernel_occupancy(rsc::k_pulse<2>, *threads, *smem, &per_sm);
     }
-    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "pulse kernel configuration: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_CUDA, "pulse kernel configuration: %s", cudaGetErrorString(e));
     if (per_sm < 1) per_sm = 1;
     if (per_sm > 4) per_sm = 4;
     if (want_per_sm > 0 && want_per_sm < per_sm) per_sm = want_per_sm;
@@ -425,7 +438,7 @@ int rsc_worker_create(int device, rsc_worker **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete w;
-        return fail(RSC_ERR_CUDA, "worker creation: %s", cudaGetErrorString(e));
+        return cuda_fail(RSC_ERR_CUDA, "worker creation: %s", cudaGetErrorString(e));
     }
     *out = w;
     return RSC_OK;
@@ -480,7 +493,7 @@ int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float 
         cudaError_t e = cudaMalloc((void **)a, b4);
         if (e != cudaSuccess) {
             free_arrays(w);
-            return fail(RSC_ERR_NOMEM, "cudaMalloc of %zu B: %s", b4, cudaGetErrorString(e));
+            return cuda_fail(RSC_ERR_NOMEM, "cudaMalloc of %zu B: %s", b4, cudaGetErrorString(e));
         }
         RSC_CUDA(cudaMemsetAsync(*a, 0, b4, w->stream));
     }
@@ -678,7 +691,7 @@ static int sort_worker(rsc_worker *w, const rsc_population *pop, const float *si
         if (e != cudaSuccess) {
             free_sort(w);
             w->sort_due = false;
-            return fail(RSC_ERR_NOMEM, "spatial-order buffers for %llu scatterers: %s", numel, cudaGetErrorString(e));
+            return cuda_fail(RSC_ERR_NOMEM, "spatial-order buffers for %llu scatterers: %s", numel, cudaGetErrorString(e));
         }
         rsc::k_iota<<<grid_of(numel, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(w->perm, numel);
         rsc::k_iota<<<grid_of(numel, rsc::kSortThreads), rsc::kSortThreads, 0, st>>>(w->inv, numel);
@@ -797,7 +810,7 @@ int step_shape(int mode, rsc_worker *w, int *grid, size_t *smem) {
     cudaError_t e = mode == RSC_PULSE_PLAIN
                         ? kernel_occupancy(rsc::k_step<0>, rsc::kAdvanceThreads, *smem, &per_sm)
                         : kernel_occupancy(rsc::k_step<1>, rsc::kAdvanceThreads, *smem, &per_sm);
-    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "step kernel configuration: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_CUDA, "step kernel configuration: %s", cudaGetErrorString(e));
     if (per_sm < 1) per_sm = 1;
     if (per_sm > 8) per_sm = 8;
     *grid = w->num_sms * per_sm;
@@ -886,7 +899,7 @@ int rsc_populate_upload(rsc_worker *w, const rsc_populate_args *args, uint32_t *
         if (hr[b]) cudaFreeHost(hr[b]);
         if (ev[b]) cudaEventDestroy(ev[b]);
     }
-    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "populate: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_CUDA, "populate: %s", cudaGetErrorString(e));
     w->sig_aux_stale = false;
     w->have_pulse_desc = false;
     w->sort_due = true;
@@ -1253,7 +1266,7 @@ namespace {
 int check_batch(rsc_batch *b) {
     if (b == nullptr) return fail(RSC_ERR_ARG, "batch is NULL");
     cudaError_t e = cudaSetDevice(b->device);
-    if (e != cudaSuccess) return fail(RSC_ERR_CUDA, "cudaSetDevice(%d): %s", b->device, cudaGetErrorString(e));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_CUDA, "cudaSetDevice(%d): %s", b->device, cudaGetErrorString(e));
     return RSC_OK;
 }
 
@@ -1280,7 +1293,7 @@ int batch_reserve(rsc_batch *b, int steps) {
     cudaError_t e = cudaMallocHost((void **)&b->h_steps, rows * sizeof(rsc::BatchStep));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_steps, rows * sizeof(rsc::BatchStep));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_out, rows * b->Gmax * sizeof(float4));
-    if (e != cudaSuccess) return fail(RSC_ERR_NOMEM, "batch buffers for %d steps: %s", steps, cudaGetErrorString(e));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_NOMEM, "batch buffers for %d steps: %s", steps, cudaGetErrorString(e));
     memset(b->h_steps, 0, rows * sizeof(rsc::BatchStep));
     RSC_CUDA(cudaMemsetAsync(b->d_out, 0, rows * b->Gmax * sizeof(float4), b->stream));
     b->cap_steps = steps;
@@ -1406,7 +1419,7 @@ int batch_capture(rsc_batch *b, int steps) {
     if (g) cudaGraphDestroy(g);
     if (e != cudaSuccess) {
         b->graph = nullptr;
-        return fail(RSC_ERR_CUDA, "graph capture of %d steps: %s", steps, cudaGetErrorString(e));
+        return cuda_fail(RSC_ERR_CUDA, "graph capture of %d steps: %s", steps, cudaGetErrorString(e));
     }
     b->graph_steps = steps;
     return RSC_OK;
@@ -1546,7 +1559,7 @@ int rsc_batch_create(rsc_worker *const *workers, int count, rsc_batch **out) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulse_prefix, (count + 1) * sizeof(unsigned));
     if (e != cudaSuccess) {
         rsc_batch_free(b);
-        return fail(RSC_ERR_CUDA, "batch creation: %s", cudaGetErrorString(e));
+        return cuda_fail(RSC_ERR_CUDA, "batch creation: %s", cudaGetErrorString(e));
     }
     *out = b;
     return RSC_OK;
@@ -1822,7 +1835,7 @@ int noalloc_scratch(void **out) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_pulse_scratch);
         if (e != cudaSuccess || p == nullptr) {
-            return fail(RSC_ERR_CUDA, "cudaGetSymbolAddress(pulse scratch) on device %d: %s", dev,
+            return cuda_fail(RSC_ERR_CUDA, "cudaGetSymbolAddress(pulse scratch) on device %d: %s", dev,
                         cudaGetErrorString(e));
         }
         g_na_addr[dev] = p;

@@ -434,3 +434,52 @@ def test_debris_flux_field_respawn(backend, oracle_lib, mode):
     moved = (st.s["rnd"][deb] != S.state["rnd"][deb]).any(axis=1)
     assert moved.sum() >= 100
     W.close()
+
+
+def test_host_fault_injection(backend, oracle_lib):
+    """Failures made on the host, none of them touching a kernel: an
+    allocation the device refuses, calls before their tables, a table whose
+    descriptor points past its end, a debris type naming a missing table.
+    Each returns its status and the worker keeps working afterwards."""
+    O = oracle_lib
+    W = backend.Worker(0)
+    with pytest.raises(backend.BackendError) as e:
+        W.malloc(2 ** 42, 1000.0, 15.0, 8)              # 70 TB: cudaMalloc refuses
+    assert e.value.status == -3
+    S = synth.make_scene(num_rain=5000, debris=[(synth.OBJ_LEAF, 64)], les_count=1, seed=5)
+    W.malloc(S.num_scats, S.range_start, S.range_delta, S.range_count)
+    W.upload(0, **S.state)
+    sd = synth.pulse_sim_desc(S, 0)
+    with pytest.raises(backend.BackendError) as e:
+        W.make_pulse(sd)                                # no range / angular weights yet
+    assert e.value.status == -4
+    bad = S.range_desc.copy()
+    bad[2] = 5.0                                        # max index past the 3-entry table
+    with pytest.raises(backend.BackendError) as e:
+        W.set_range_weight(S.range_w, bad)
+    assert e.value.status == -1
+    W.set_range_weight(S.range_w, S.range_desc)
+    W.set_angular_weight(S.ang_w, S.ang_desc)
+    W.set_rcs_ellipsoid(S.ell, S.ell_desc)
+    pop = synth.population(S)
+    with pytest.raises(backend.BackendError) as e:
+        W.advance_time(pop, 0, sd)                      # no LES volume yet
+    assert e.value.status == -4
+    W.set_les(0, S.les[0].uvwt, S.les[0].cpxx, S.les_desc)
+    with pytest.raises(backend.BackendError) as e:
+        W.advance_time(pop, 0, sd)                      # the leaf's ADM table is missing
+    assert e.value.status == -4
+    for t, (cd, cm, ad) in enumerate(S.adm):
+        W.set_adm(t, cd, cm, ad)
+    for t, (re, im, rd) in enumerate(S.rcs_tables):
+        W.set_rcs(t, re, im, rd)
+    # after all of that, a normal step matches the oracle
+    st = O.OracleState(S.state)
+    W.make_pulse(sd)
+    g = W.download_pulse(1.0)
+    d, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+    assert_pulse_close(g, d, ab, "after the failures")
+    W.advance_time(pop, 0, sd)
+    O.advance_time(st, S, S.counts, S.les[0], sd)
+    assert_state_equal(W.download(STATE_FIELDS), st.s, where="after the failures ")
+    W.close()
