@@ -127,6 +127,8 @@ struct rsc_worker {
      * rsc_make_pulse runs it together with the pulse (k_step); any other call
      * that reads or changes the state or the tables runs it alone first */
     int fuse = 0;
+    cudaStream_t side = nullptr;             /* debris kernel beside the background kernel */
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     bool pend = false;
     AdvanceArgs pend_a;
     unsigned pend_blocks = 0;
@@ -237,7 +239,7 @@ Image make_image(const float4 *d, uint32_t nx, uint32_t ny, uint32_t nz) {
     return im;
 }
 
-/* Debris launch description shared by k_advance and k_db_rcs. */
+/* Debris launch description shared by the advance kernels and k_db_rcs. */
 int fill_debris(rsc_worker *w, const rsc_population *pop, AdvanceArgs &a, unsigned long long *total) {
     a.ntypes = 0;
     unsigned long long acc = 0;
@@ -344,6 +346,40 @@ int pulse_geometry(rsc_worker *w, int mode, int *grid, int *threads, size_t *sme
     return RSC_OK;
 }
 
+/* One time step: the background kernel (its mode chosen at compile time) on
+ * the worker's stream and the debris kernel beside it on the side stream,
+ * joined back before anything later on the worker's stream.  Returns the
+ * number of launches. */
+cudaError_t launch_advance(rsc_worker *w, const AdvanceArgs &a, unsigned blocks, int *launched) {
+    const unsigned deb_blocks = blocks - a.rain_blocks;
+    cudaError_t e = cudaSuccess;
+    *launched = 0;
+    if (deb_blocks) {
+        e = cudaEventRecord(w->fork_ev, w->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(w->side, w->fork_ev, 0);
+        if (e != cudaSuccess) return e;
+        rsc::k_advance_debris<<<deb_blocks, rsc::kAdvanceThreads, 0, w->side>>>(a);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(w->join_ev, w->side);
+        if (e != cudaSuccess) return e;
+        (*launched)++;
+    }
+    if (a.rain_blocks) {
+        if (a.rain_mode == 1) {
+            rsc::k_advance_rain<1><<<a.rain_blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
+        } else if (a.rain_mode == 0) {
+            rsc::k_advance_rain<0><<<a.rain_blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
+        } else {
+            rsc::k_advance_rain<2><<<a.rain_blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        (*launched)++;
+    }
+    if (deb_blocks) e = cudaStreamWaitEvent(w->stream, w->join_ev, 0);
+    return e;
+}
+
 void launch_pulse(int mode, const PulseArgs &P, int grid, int threads, size_t smem, cudaStream_t st) {
     if (mode == RSC_PULSE_PLAIN) {
         rsc::k_pulse<0><<<grid, threads, smem, st>>>(P);
@@ -436,6 +472,9 @@ int rsc_worker_create(int device, rsc_worker **out) {
     w->device = device;
     cudaError_t e = cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->join_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete w;
         return cuda_fail(RSC_ERR_CUDA, "worker creation: %s", cudaGetErrorString(e));
@@ -463,6 +502,12 @@ int rsc_worker_free(rsc_worker *w) {
         free_ptr(w->rcs_tab[t].a);
         free_ptr(w->rcs_tab[t].b);
     }
+    if (w->side) {
+        cudaStreamSynchronize(w->side);
+        cudaStreamDestroy(w->side);
+    }
+    if (w->fork_ev) cudaEventDestroy(w->fork_ev);
+    if (w->join_ev) cudaEventDestroy(w->join_ev);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
     return RSC_OK;
@@ -789,14 +834,14 @@ static int maybe_sort(rsc_worker *w, const rsc_population *pop, const float *sim
 
 namespace {
 
-/* Run a recorded advance on its own (k_advance) and do its bookkeeping. */
+/* Run a recorded advance on its own and do its bookkeeping. */
 int flush_pending(rsc_worker *w) {
     if (!w->pend) return RSC_OK;
     w->pend = false;
     if (w->pend_blocks) {
-        rsc::k_advance<<<w->pend_blocks, rsc::kAdvanceThreads, 0, w->stream>>>(w->pend_a);
-        RSC_CUDA(cudaGetLastError());
-        w->launches++;
+        int n = 0;
+        RSC_CUDA(launch_advance(w, w->pend_a, w->pend_blocks, &n));
+        w->launches += n;
     }
     w->since_sort++;
     return maybe_sort(w, &w->pend_pop, w->pend_sim, w->stream);
@@ -1061,9 +1106,9 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
         w->sig_aux_stale = true;
         return RSC_OK;
     }
-    rsc::k_advance<<<blocks, rsc::kAdvanceThreads, 0, w->stream>>>(a);
-    RSC_CUDA(cudaGetLastError());
-    w->launches++;
+    int n = 0;
+    RSC_CUDA(launch_advance(w, a, blocks, &n));
+    w->launches += n;
     w->sig_aux_stale = true;
     w->since_sort++;
     return maybe_sort(w, pop, sim_desc, w->stream);

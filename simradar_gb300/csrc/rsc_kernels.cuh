@@ -1,9 +1,11 @@
 /*
  * rsc_kernels.cuh -- the sm_103a kernels of the emulation loop.
  *
- *   k_advance     one launch per time step: el_atts / bg_atts / fp_atts on the
- *                 background range and db_atts on every debris range
- *                 (rs.cl:533-907), one thread per scatterer, float4 loads.
+ *   k_advance_rain    one time step of the background range: el_atts /
+ *                     bg_atts / fp_atts (rs.cl:533-739), one thread per
+ *                     scatterer, float4 loads, the kernel chosen by concept.
+ *   k_advance_debris  db_atts on every debris range (rs.cl:744-907) in one
+ *                     launch, run beside the background kernel.
  *   k_db_rcs      debris RCS refresh after a beam move (rs.cl:909-919).
  *   k_sig_aux     forms aux / sig for RS_download when the pulse kernel did
  *                 not write them.
@@ -297,16 +299,18 @@ __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned lon
  * background, the rest the debris types in order): advanced in memory, and
  * its new position and backscatter returned for a pulse formed in the same
  * pass.  False when the thread has no scatterer. */
-__device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, unsigned long long &i_out, float4 &pos,
-                                            float4 &rcs) {
+template <int RAIN_MODE>   /* 0 bg_atts, 1 el_atts, 2 fp_atts, -1 chosen by a.rain_mode */
+__device__ __forceinline__ bool advance_one_t(const AdvanceArgs &a, unsigned b, unsigned long long &i_out,
+                                              float4 &pos, float4 &rcs) {
     bool known = true;
     if (b < a.rain_blocks) {
         unsigned long long j = (unsigned long long)b * kAdvanceThreads + threadIdx.x;
         if (j >= a.rain_count) return false;
         size_t i = (size_t)(a.rain_origin + j);
-        if (a.rain_mode == 1) {
+        const int mode = RAIN_MODE >= 0 ? RAIN_MODE : a.rain_mode;
+        if (mode == 1) {
             rain_el(a, i, pos, rcs, known);
-        } else if (a.rain_mode == 0) {
+        } else if (mode == 0) {
             rain_bg(a, i, pos, rcs, known);
         } else {
             rain_fp(a, i, pos, rcs, known);
@@ -325,6 +329,11 @@ __device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, un
     return true;
 }
 
+__device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, unsigned long long &i_out, float4 &pos,
+                                            float4 &rcs) {
+    return advance_one_t<-1>(a, b, i_out, pos, rcs);
+}
+
 __device__ __forceinline__ void advance_body(const AdvanceArgs &a, unsigned b) {
     unsigned long long i;
     float4 pos, rcs;
@@ -334,8 +343,35 @@ __device__ __forceinline__ void advance_body(const AdvanceArgs &a, unsigned b) {
 /* 5 blocks of 256 per SM (<= 51 registers): the step is a chain of dependent
  * loads (state, then 8 LES texels, then the debris tables), so resident warps
  * are what hides the latency */
-__global__ void __launch_bounds__(kAdvanceThreads, 5) k_advance(const AdvanceArgs a) {
-    advance_body(a, blockIdx.x);
+/* One time step as two kernels: the background kernel holds only its own
+ * (short) path, which the debris path's code slows by about a tenth when both
+ * share one kernel; the host runs the debris kernel beside it on a second
+ * stream.  The batched and fused kernels take both paths through
+ * advance_one. */
+template <int RAIN_MODE>
+__global__ void __launch_bounds__(kAdvanceThreads, 6) k_advance_rain(const AdvanceArgs a) {
+    const unsigned long long j = (unsigned long long)blockIdx.x * kAdvanceThreads + threadIdx.x;
+    if (j >= a.rain_count) return;
+    const size_t i = (size_t)(a.rain_origin + j);
+    float4 pos, rcs;
+    bool known;
+    if (RAIN_MODE == 1) {
+        rain_el(a, i, pos, rcs, known);
+    } else if (RAIN_MODE == 0) {
+        rain_bg(a, i, pos, rcs, known);
+    } else {
+        rain_fp(a, i, pos, rcs, known);
+    }
+}
+
+__global__ void __launch_bounds__(kAdvanceThreads) k_advance_debris(const AdvanceArgs a) {
+    const unsigned long long j = (unsigned long long)blockIdx.x * kAdvanceThreads + threadIdx.x;
+    if (a.ntypes == 0 || j >= a.deb_prefix[a.ntypes]) return;
+    const int t = debris_type_of(a, j);
+    const DebrisType &T = a.types[t];
+    float4 pos, rcs;
+    bool known;
+    debris_step(a, T, (size_t)(T.origin + (j - a.deb_prefix[t])), pos, rcs, known);
 }
 
 /* ---- db_rcs (rs.cl:909-919) for every debris type ---- */

@@ -8,7 +8,7 @@
  * of read again by a separate pulse kernel.  The grid is persistent (a few
  * blocks per SM, each looping over the advance's blocks of 256 scatterers)
  * so that every block's gate bins are added to the FP64 accumulator once.
- * Results are those of k_advance followed by k_pulse: the same per-scatterer
+ * Results are those of the advance kernels followed by k_pulse: the same per-scatterer
  * operations, the gate sums in another order.
  */
 #ifndef SIMRADAR_GB300_RSC_STEP_CUH
