@@ -243,7 +243,13 @@ __device__ __forceinline__ void warp_reduce4_add_df(float *df, unsigned lane, fl
     }
 }
 
-template <int MODE>
+/* PATH: 0 sparse gates with per-lane atomics (state in the caller's order),
+ * 1 sparse gates, summed across the warp where its lanes share a few gates
+ * (state in spatial order), per-lane atomics elsewhere, 2 every gate (a range
+ * weight with non-zero edges), -1 chosen at run time from the arguments (the
+ * batched and fused kernels).  A kernel compiled for one path holds only that
+ * path's code. */
+template <int MODE, int PATH = -1>
 struct PulseBins {
     typedef PulseTraits<MODE> Tr;
     typedef typename Tr::Acc Acc;
@@ -321,7 +327,7 @@ struct PulseBins {
                 }
             }
         }
-        if (!P.dense) {
+        if (PATH == 2 ? false : (PATH >= 0 ? true : !P.dense)) {
             /* candidate gates: only those the range weight can reach */
             int k_lo = 0, k_hi = -1;
             if (in && finite) {
@@ -344,7 +350,7 @@ struct PulseBins {
                     }
                     bin_add<Acc>(wbins, 0xffffffffu, nz, gate, cw);
                 }
-            } else if ((coherent = warp_coherent(in && finite, k_lo, k_hi, P.coherent_span, w_lo, w_hi))) {
+            } else if (PATH != 0 && (coherent = warp_coherent(in && finite, k_lo, k_hi, P.coherent_span, w_lo, w_hi))) {
                 /* the warp's candidates fall in a few gates (a state kept in
                  * spatial order): visit them together and reduce each gate
                  * across the warp, no atomics.  The gate origin is advanced
@@ -509,9 +515,9 @@ struct PulseBins {
     }
 };
 
-template <int MODE>
+template <int MODE, int PATH = -1>
 __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, unsigned nblk) {
-    PulseBins<MODE> B;
+    PulseBins<MODE, PATH> B;
     B.init(P);
     const unsigned long long stride = (unsigned long long)nblk * blockDim.x;
     const unsigned long long n = P.n;
@@ -531,9 +537,9 @@ __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, uns
     B.finish(P, nblk);
 }
 
-template <int MODE>
+template <int MODE, int PATH>
 __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
-    pulse_body<MODE>(P, blockIdx.x, gridDim.x);
+    pulse_body<MODE, PATH>(P, blockIdx.x, gridDim.x);
 }
 
 }  // namespace rsc
