@@ -340,6 +340,62 @@ int rsc_iq_flush(rsc_iq_writer *w);
 int rsc_iq_close(rsc_iq_writer *w);
 const char *rsc_iq_last_error(void);
 
+/* ---- LES frame source (additive) ----
+ * The LES ingest of les.c: the grid file fort.10_2 (les.c:477-518) and the
+ * frame files LES_mean_1_6_fnum<k>.dat (k = 1, 2, ...; 10 volumes each, every
+ * volume a time stamp and the u, v, w, p, t planes as Fortran records,
+ * les.c:318-422) in one LES folder (<tables>/les/<config>, the folder
+ * LES_init_with_config_path finds), the per-config constants of
+ * les.c:158-208 and the remap of les.c:388-406 (u, v, w scaled by v0 into
+ * uvwt with t * t0; p * p0 into cpxx lane 1, or lane 0 for "flat").  A
+ * background thread reads the frame after the last one asked for, as
+ * LES_background_read does; rsc_les_upload_async sends a frame's raw planes
+ * (20 B per cell instead of the 32 B of uvwt + cpxx) to the device on a copy
+ * stream and remaps them there, so the frame swap of RS_advance_time
+ * (rs.c:5188-5200) overlaps the pulse loop. */
+typedef struct {
+    uint32_t nx, ny, nz;          /* cells per axis (the data grid, les.c:520-547) */
+    uint32_t files;               /* frame files found */
+    uint32_t volumes_per_file;    /* from the first file's size (les.c:212-244) */
+    uint32_t frames;              /* files x volumes_per_file (LES_get_table_count) */
+    int32_t is_stretched;         /* stretched grid (suctvort, suctvort_large) */
+    int32_t p_for_cn2;            /* p goes to cpxx lane 0 (config "flat") */
+    float tr, tp;                 /* refresh time, period of a frame (LES_get_table_period) */
+    float v0, p0, t0;             /* scale of u, v, w / p / t */
+    float ax, ay, az, rx, ry, rz; /* stretched: a r^n series; uniform: rx..rz = spacing */
+} rsc_les_info;
+typedef struct rsc_les_source rsc_les_source;
+
+/* Open the LES folder `dir` (holding fort.10_2 and the frame files) with the
+ * constants of `config` ("suctvort", "suctvort_large", "twocell", "flat" or
+ * any other name, les.c:159-208) and start the read-ahead thread. */
+int rsc_les_open(const char *dir, const char *config, rsc_les_source **out);
+int rsc_les_get_info(rsc_les_source *src, rsc_les_info *info);
+/* The data grid's node coordinates, nx * ny * nz floats each (LESTable
+ * data.x / .y / .z); NULL skips an axis. */
+int rsc_les_grid(rsc_les_source *src, float *x, float *y, float *z);
+/* The 16-float LES descriptor RS_set_vel_data_to_LES_table (rs.c:3029-3126)
+ * and RS_set_vel_data (rs.c:2947-2976) derive from the table constants. */
+int rsc_les_descriptor(const rsc_les_info *info, float desc[16]);
+/* Frame `frame` (0 .. frames-1) remapped into host uvwt4 / cpxx4 arrays of
+ * nx * ny * nz float4 (LES_get_frame, les.c:666-694); *time (may be NULL)
+ * gets the frame's time stamp.  The frame after it is read ahead. */
+int rsc_les_read(rsc_les_source *src, uint32_t frame, float *uvwt4, float *cpxx4, float *time);
+/* Start reading `frame` on the background thread. */
+int rsc_les_prefetch(rsc_les_source *src, uint32_t frame);
+/* Frame `frame` into LES slot `slot` of the worker (allocating the slots as
+ * rsc_set_les does) with the descriptor of rsc_les_descriptor: the raw
+ * planes go to the device on the worker's copy stream while earlier work
+ * runs, the remap kernel writes the slot after the work queued so far on
+ * the worker, and the first later advance that reads the slot waits for it.
+ * The next frame is read ahead. */
+int rsc_les_upload_async(rsc_worker *w, rsc_les_source *src, int slot, uint32_t frame, float *time);
+/* Stop the thread, wait for copies out of the source's buffers, free it. */
+int rsc_les_close(rsc_les_source *src);
+/* Message of the last failed rsc_les_* call of this thread other than
+ * rsc_les_upload_async, which reports through rsc_last_error. */
+const char *rsc_les_last_error(void);
+
 /* Limits of rsc_make_pulse_noalloc (its scratch is a fixed device array of
  * about 9 KB per GPU that loads this library). */
 #define RSC_NOALLOC_MAX_GATES 128

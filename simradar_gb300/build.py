@@ -13,8 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libsimradar_gb300.so")
-SOURCES = ["rsc.cu", "rsc_iq.cpp", "rsc_populate.cpp"]
-DEPS = ["rsc.cu", "rsc_iq.cpp", "rsc_populate.cpp", "rsc_populate.h", "rsc_batch.cuh", "rsc_sort.cuh", "rsc_step.cuh", "rsc_pulse.cuh", "rsc_kernels.cuh", "rsc_physics.cuh", "rsmath.h"]
+SOURCES = ["rsc.cu", "rsc_iq.cpp", "rsc_populate.cpp", "rsc_les.cpp"]
+DEPS = ["rsc.cu", "rsc_iq.cpp", "rsc_populate.cpp", "rsc_populate.h", "rsc_les.cpp", "rsc_les.h", "rsc_batch.cuh", "rsc_sort.cuh", "rsc_step.cuh", "rsc_pulse.cuh", "rsc_kernels.cuh", "rsc_physics.cuh", "rsmath.h"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 

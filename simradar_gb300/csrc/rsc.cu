@@ -18,6 +18,7 @@
 #include "../../include/rsc.h"
 #include "rsc_batch.cuh"
 #include "rsc_sort.cuh"
+#include "rsc_les.h"
 #include "rsc_populate.h"
 
 using rsc::AdvanceArgs;
@@ -100,6 +101,14 @@ struct rsc_worker {
     float4 *les_uvwt[2] = {nullptr, nullptr}, *les_cpxx[2] = {nullptr, nullptr};
     uint32_t les_nx = 0, les_ny = 0, les_nz = 0;
     float les_desc[16] = {0};
+    /* LES frames from an rsc_les_source: raw planes copied on les_copy into
+     * les_raw and remapped into a slot; les_ready[slot] marks the slot
+     * written, les_wait[slot] that no advance has waited for it yet */
+    cudaStream_t les_copy = nullptr;
+    cudaEvent_t les_mark = nullptr, les_ready[2] = {nullptr, nullptr};
+    bool les_wait[2] = {false, false};
+    float *les_raw = nullptr;
+    size_t les_raw_n = 0;
     Table2D adm[RSC_MAX_TYPES];
     Table2D rcs_tab[RSC_MAX_TYPES];
     float *dff[2] = {nullptr, nullptr};
@@ -495,6 +504,7 @@ int rsc_worker_free(rsc_worker *w) {
     if (w == nullptr) return RSC_OK;
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
+    if (w->les_copy) cudaStreamSynchronize(w->les_copy);
     free_arrays(w);
     free_ptr(w->range_weight);
     free_ptr(w->angular_weight);
@@ -509,6 +519,15 @@ int rsc_worker_free(rsc_worker *w) {
         free_ptr(w->adm[t].b);
         free_ptr(w->rcs_tab[t].a);
         free_ptr(w->rcs_tab[t].b);
+    }
+    if (w->les_copy) {
+        cudaStreamSynchronize(w->les_copy);
+        cudaStreamDestroy(w->les_copy);
+    }
+    free_ptr(w->les_raw);
+    if (w->les_mark) cudaEventDestroy(w->les_mark);
+    for (int s = 0; s < 2; s++) {
+        if (w->les_ready[s]) cudaEventDestroy(w->les_ready[s]);
     }
     if (w->side) {
         cudaStreamSynchronize(w->side);
@@ -620,19 +639,23 @@ int rsc_set_rcs_ellipsoid(rsc_worker *w, const float *table4, uint32_t n, const 
     return RSC_OK;
 }
 
-static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny,
-                        uint32_t nz, const float desc[16], bool async) {
-    int s = check_worker(w);
-    if (s) return s;
-    s = flush_pending(w);
-    if (s) return s;
-    if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
-    if (uvwt4 == nullptr || desc == nullptr || nx == 0 || ny == 0 || nz == 0) return fail(RSC_ERR_ARG, "LES table");
+/* Make the worker's stream wait for a pending remap into LES slot `slot`. */
+static int les_slot_wait(rsc_worker *w, int slot) {
+    if (!w->les_wait[slot]) return RSC_OK;
+    RSC_CUDA(cudaStreamWaitEvent(w->stream, w->les_ready[slot], 0));
+    w->les_wait[slot] = false;
+    return RSC_OK;
+}
+
+/* Both LES slots allocated for nx x ny x nz texels. */
+static int ensure_les_slots(rsc_worker *w, uint32_t nx, uint32_t ny, uint32_t nz) {
     const size_t nn = (size_t)nx * ny * nz;
     if (nn >= (1ull << 31)) return fail(RSC_ERR_UNSUPPORTED, "LES of %zu texels (the kernels index below 2^31)", nn);
     if (w->les_uvwt[0] != nullptr && (nx != w->les_nx || ny != w->les_ny || nz != w->les_nz)) {
         /* new dimensions: reallocate both slots (rs.c:3000-3016 releases them) */
         cudaStreamSynchronize(w->stream);
+        if (w->les_copy) cudaStreamSynchronize(w->les_copy);
+        w->les_wait[0] = w->les_wait[1] = false;
         for (int k = 0; k < 2; k++) {
             free_ptr(w->les_uvwt[k]);
             free_ptr(w->les_cpxx[k]);
@@ -649,6 +672,22 @@ static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float
         w->les_ny = ny;
         w->les_nz = nz;
     }
+    return RSC_OK;
+}
+
+static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny,
+                        uint32_t nz, const float desc[16], bool async) {
+    int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
+    if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
+    if (uvwt4 == nullptr || desc == nullptr || nx == 0 || ny == 0 || nz == 0) return fail(RSC_ERR_ARG, "LES table");
+    s = ensure_les_slots(w, nx, ny, nz);
+    if (s) return s;
+    s = les_slot_wait(w, slot);
+    if (s) return s;
+    const size_t nn = (size_t)nx * ny * nz;
     RSC_CUDA(cudaMemcpyAsync(w->les_uvwt[slot], uvwt4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
     if (cpxx4) {
         RSC_CUDA(cudaMemcpyAsync(w->les_cpxx[slot], cpxx4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
@@ -666,6 +705,58 @@ int rsc_set_les(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4,
 int rsc_set_les_async(rsc_worker *w, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx, uint32_t ny,
                       uint32_t nz, const float desc[16]) {
     return set_les_impl(w, slot, uvwt4, cpxx4, nx, ny, nz, desc, true);
+}
+
+int rsc_les_upload_async(rsc_worker *w, rsc_les_source *src, int slot, uint32_t frame, float *time) {
+    int s = check_worker(w);
+    if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
+    if (src == nullptr) return fail(RSC_ERR_ARG, "LES source is NULL");
+    if (slot < 0 || slot > 1) return fail(RSC_ERR_ARG, "LES slot %d", slot);
+    const rsc_les_info &I = rscles::info(src);
+    if (frame >= I.frames) return fail(RSC_ERR_ARG, "LES frame %u of %u", frame, I.frames);
+    s = ensure_les_slots(w, I.nx, I.ny, I.nz);
+    if (s) return s;
+    const size_t nn = (size_t)I.nx * I.ny * I.nz;
+    if (w->les_copy == nullptr) {
+        RSC_CUDA(cudaStreamCreateWithFlags(&w->les_copy, cudaStreamNonBlocking));
+        RSC_CUDA(cudaEventCreateWithFlags(&w->les_mark, cudaEventDisableTiming));
+        for (int k = 0; k < 2; k++) RSC_CUDA(cudaEventCreateWithFlags(&w->les_ready[k], cudaEventDisableTiming));
+    }
+    if (w->les_raw_n != 5 * nn) {
+        /* the staging buffer is reused in copy-stream order */
+        RSC_CUDA(cudaStreamSynchronize(w->les_copy));
+        free_ptr(w->les_raw);
+        w->les_raw = nullptr;
+        w->les_raw_n = 0;
+        cudaError_t e = cudaMalloc((void **)&w->les_raw, 5 * nn * sizeof(float));
+        if (e != cudaSuccess) return cuda_fail(RSC_ERR_NOMEM, "LES staging of %zu MB: %s", 5 * nn * 4 >> 20, cudaGetErrorString(e));
+        w->les_raw_n = 5 * nn;
+    }
+    rscles::Held h;
+    const char *why = "";
+    s = rscles::acquire(src, frame, &h, &why);
+    if (s) return fail(s, "LES frame %u: %s", frame, why);
+    if (rscles::pin(src, h, &why) != RSC_OK) {
+        /* pageable: the copy is staged by the driver, still correct */
+    }
+    cudaError_t e = cudaMemcpyAsync(w->les_raw, h.planes, 5 * nn * sizeof(float), cudaMemcpyHostToDevice, w->les_copy);
+    rscles::release(src, h, e == cudaSuccess ? w->les_copy : nullptr);
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_CUDA, "LES frame copy: %s", cudaGetErrorString(e));
+    /* the slot is rewritten after the work queued on the worker so far */
+    RSC_CUDA(cudaEventRecord(w->les_mark, w->stream));
+    RSC_CUDA(cudaStreamWaitEvent(w->les_copy, w->les_mark, 0));
+    const int grid = w->num_sms * 8;
+    rsc::k_les_remap<<<grid, 256, 0, w->les_copy>>>(w->les_raw, nn, I.v0, I.p0, I.t0, I.p_for_cn2, w->les_uvwt[slot],
+                                                    w->les_cpxx[slot]);
+    RSC_CUDA(cudaGetLastError());
+    RSC_CUDA(cudaEventRecord(w->les_ready[slot], w->les_copy));
+    w->les_wait[slot] = true;
+    w->launches++;
+    rsc_les_descriptor(&I, w->les_desc);
+    if (time) *time = h.time;
+    return RSC_OK;
 }
 
 static int set_table2d(rsc_worker *w, Table2D *t, const float *a4, const float *b4, uint32_t nx, uint32_t ny,
@@ -1104,6 +1195,8 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
     s = fill_advance_args(w, pop, les_id, sim_desc, a, &blocks);
     if (s) return s;
     if (blocks == 0) return RSC_OK;
+    s = les_slot_wait(w, les_id);
+    if (s) return s;
     if (w->fuse && w->precision != RSC_PULSE_F64) {
         /* run with the next pulse, or alone by the next call that needs it */
         w->pend = true;
@@ -1746,6 +1839,12 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
         if (used[q] && b->slot_pending[q]) {
             RSC_CUDA(cudaStreamWaitEvent(b->stream, b->slot_ready[q], 0));
             b->slot_pending[q] = 0;
+        }
+        rsc_worker *x = b->w[q / 2];
+        if (used[q] && x->les_wait[q & 1]) {
+            /* a frame from rsc_les_upload_async */
+            RSC_CUDA(cudaStreamWaitEvent(b->stream, x->les_ready[q & 1], 0));
+            x->les_wait[q & 1] = false;
         }
     }
     RSC_CUDA(cudaMemcpyAsync(b->d_steps, b->h_steps, (size_t)steps * n * sizeof(rsc::BatchStep),

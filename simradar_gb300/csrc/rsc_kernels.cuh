@@ -9,6 +9,7 @@
  *   k_db_rcs      debris RCS refresh after a beam move (rs.cl:909-919).
  *   k_sig_aux     forms aux / sig for RS_download when the pulse kernel did
  *                 not write them.
+ *   k_les_remap   scales an LES frame's raw planes into a uvwt / cpxx slot.
  * plus the pieces the pulse kernel (rsc_pulse.cuh) is built from: the
  * pass-1 weights, the per-scatterer signal and the per-warp gate bins.
  */
@@ -619,6 +620,23 @@ __global__ void __launch_bounds__(256) k_sig_aux(const PulseArgs P) {
     ax.w = sg.wang;
     P.aux[i] = ax;
     P.sig[i] = make_float4(sg.sig[0], sg.sig[1], sg.sig[2], sg.sig[3]);
+}
+
+/* The remap of an LES frame (les.c:388-406): the file's u, v, w, p, t
+ * planes (nn floats each) scaled into uvwt = (u v0, v v0, w v0, t t0) and
+ * cpxx = (0, p p0, 0, 0), or (p p0, 0, 0, 0) when p is the cn2 of the flat
+ * configuration.  Reads 20 B and writes 32 B per cell, coalesced. */
+__global__ void __launch_bounds__(256) k_les_remap(const float *__restrict__ raw, size_t nn, float v0, float p0,
+                                                   float t0, int p_for_cn2, float4 *__restrict__ uvwt,
+                                                   float4 *__restrict__ cpxx) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += stride) {
+        const float u = __ldg(raw + k), v = __ldg(raw + nn + k), w = __ldg(raw + 2 * nn + k);
+        const float p = __ldg(raw + 3 * nn + k), t = __ldg(raw + 4 * nn + k);
+        uvwt[k] = make_float4(u * v0, v * v0, w * v0, t * t0);
+        const float pp = p * p0;
+        cpxx[k] = p_for_cn2 ? make_float4(pp, 0.0f, 0.0f, 0.0f) : make_float4(0.0f, pp, 0.0f, 0.0f);
+    }
 }
 
 /* diagnostics */

@@ -519,3 +519,103 @@ def populate_upload(worker, args):
     pop = np.zeros(max(1, args.dsd_count), np.uint32)
     _check(L.rsc_populate_upload(worker._h, ctypes.byref(args), pop.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
     return pop[:args.dsd_count]
+
+
+class LESInfo(ctypes.Structure):
+    """rsc_les_info: dimensions, frame count and constants of an LES folder."""
+    _fields_ = [("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("nz", ctypes.c_uint32),
+                ("files", ctypes.c_uint32), ("volumes_per_file", ctypes.c_uint32), ("frames", ctypes.c_uint32),
+                ("is_stretched", ctypes.c_int32), ("p_for_cn2", ctypes.c_int32),
+                ("tr", ctypes.c_float), ("tp", ctypes.c_float),
+                ("v0", ctypes.c_float), ("p0", ctypes.c_float), ("t0", ctypes.c_float),
+                ("ax", ctypes.c_float), ("ay", ctypes.c_float), ("az", ctypes.c_float),
+                ("rx", ctypes.c_float), ("ry", ctypes.c_float), ("rz", ctypes.c_float)]
+
+
+def _les_lib():
+    L = load_library()
+    P, I, U32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32
+    for name, argtypes in {
+        "rsc_les_open": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(P)],
+        "rsc_les_get_info": [P, ctypes.POINTER(LESInfo)],
+        "rsc_les_grid": [P, _f32p, _f32p, _f32p],
+        "rsc_les_descriptor": [ctypes.POINTER(LESInfo), _f32p],
+        "rsc_les_read": [P, U32, _f32p, _f32p, _f32p],
+        "rsc_les_prefetch": [P, U32],
+        "rsc_les_upload_async": [P, P, I, U32, _f32p],
+        "rsc_les_close": [P],
+    }.items():
+        fn = getattr(L, name)
+        fn.argtypes = argtypes
+        fn.restype = I
+    L.rsc_les_last_error.restype = ctypes.c_char_p
+    return L
+
+
+class LESSource:
+    """An LES folder of les.c (fort.10_2 + LES_mean_1_6_fnum<k>.dat) with a
+    read-ahead thread: host frames (read) or device slots (upload_async)."""
+
+    def __init__(self, directory, config="suctvort"):
+        self._lib = _les_lib()
+        self._h = ctypes.c_void_p()
+        self._check(self._lib.rsc_les_open(os.fsencode(directory), config.encode(), ctypes.byref(self._h)))
+        self.info = LESInfo()
+        self._check(self._lib.rsc_les_get_info(self._h, ctypes.byref(self.info)))
+
+    def _check(self, st):
+        if st != RSC_OK:
+            raise BackendError(st, self._lib.rsc_les_last_error().decode(errors="replace"))
+
+    @property
+    def shape(self):
+        return (self.info.nz, self.info.ny, self.info.nx)
+
+    @property
+    def frames(self):
+        return self.info.frames
+
+    def descriptor(self):
+        d = np.zeros(16, np.float32)
+        self._check(self._lib.rsc_les_descriptor(ctypes.byref(self.info), _fp(d)))
+        return d
+
+    def grid(self):
+        x, y, z = (np.zeros(self.shape, np.float32) for _ in range(3))
+        self._check(self._lib.rsc_les_grid(self._h, _fp(x), _fp(y), _fp(z)))
+        return x, y, z
+
+    def read(self, frame):
+        """(uvwt, cpxx, time) of a frame, remapped as les.c does."""
+        uvwt = np.zeros(self.shape + (4,), np.float32)
+        cpxx = np.zeros(self.shape + (4,), np.float32)
+        t = ctypes.c_float(0.0)
+        self._check(self._lib.rsc_les_read(self._h, int(frame), _fp(uvwt), _fp(cpxx), ctypes.byref(t)))
+        return uvwt, cpxx, t.value
+
+    def prefetch(self, frame):
+        self._check(self._lib.rsc_les_prefetch(self._h, int(frame)))
+
+    def upload_async(self, worker, slot, frame):
+        """Frame into a worker's LES slot (copy stream + remap kernel); returns
+        the frame's time stamp."""
+        t = ctypes.c_float(0.0)
+        _check(self._lib.rsc_les_upload_async(worker._h, self._h, int(slot), int(frame), ctypes.byref(t)))
+        return t.value
+
+    def close(self):
+        if self._h:
+            self._lib.rsc_les_close(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

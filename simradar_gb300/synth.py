@@ -22,6 +22,7 @@ RS_set_angular_weight_to_standard (rs.c:2826-2852), RS_compute_rcs_ellipsoids
 (rs.c:5922-6030), ADM_compute_properties (adm.c:279-304).
 """
 import math
+import os
 import struct
 
 import numpy as np
@@ -128,6 +129,48 @@ def les_volumes(cfg=None, count=10, seed=1, vmax=50.0, core=100.0, sigma=3.0, in
         cpxx[..., 1] = p0
         vols.append(LESVolume(uvwt, cpxx))
     return cfg, vols
+
+
+LES_SCALES = {"suctvort": (100.0, 1.0e4, 1.0e4), "suctvort_large": (100.0, 1.0e4, 1.0e4),
+              "twocell": (225.0, 225.0 ** 2, 225.0 ** 2), "flat": (100.0, 1.0, 1.0e4)}
+
+
+def write_les_folder(directory, cfg, vols, config="suctvort", volumes_per_file=10, node_km=None):
+    """Write volumes in the files les.c reads (an LES folder): fort.10_2 with
+    the node coordinates (km) and LES_mean_1_6_fnum<k>.dat with
+    `volumes_per_file` volumes each, u v w p t divided by the configuration's
+    scales (les.c:158-208), Fortran record markers around every field.  The
+    synthetic stand-in for the LES tables the reference downloads."""
+    os.makedirs(directory, exist_ok=True)
+    nx, ny, nz = cfg.nx, cfg.ny, cfg.nz
+    nn = nx * ny * nz
+    if node_km is None:
+        x, y, z = cfg.node_positions()
+        Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+        node_km = (X * 1e-3, Y * 1e-3, Z * 1e-3)
+
+    def marker(n):
+        return np.array([n], np.uint32).tobytes()
+
+    with open(os.path.join(directory, "fort.10_2"), "wb") as f:
+        f.write(marker(12) + np.array([nx, ny, nz], np.uint32).tobytes() + marker(12))
+        for a in node_km:
+            f.write(marker(4 * nn) + np.ascontiguousarray(a, np.float32).tobytes() + marker(4 * nn))
+    v0, p0, t0 = LES_SCALES.get(config.lower(), (100.0, 1.0e4, 1.0e4))
+    cn2 = config == "flat"
+    for first in range(0, len(vols), volumes_per_file):
+        path = os.path.join(directory, "LES_mean_1_6_fnum%d.dat" % (first // volumes_per_file + 1))
+        with open(path, "wb") as f:
+            f.write(marker(4))
+            for k, vol in enumerate(vols[first:first + volumes_per_file]):
+                t = np.float32((first + k) * float(cfg.tp))
+                planes = [vol.uvwt[..., 0] / v0, vol.uvwt[..., 1] / v0, vol.uvwt[..., 2] / v0,
+                          (vol.cpxx[..., 0] if cn2 else vol.cpxx[..., 1]) / p0, vol.uvwt[..., 3] / t0]
+                f.write(t.tobytes() + marker(4) + marker(4 * nn))
+                for j, a in enumerate(planes):
+                    last = j == len(planes) - 1
+                    f.write(np.ascontiguousarray(a, np.float32).tobytes() + marker(4 * nn) +
+                            marker(4 if last else 4 * nn))
 
 
 # ---------------------------------------------------------------- debris tables

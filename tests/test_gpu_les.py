@@ -1,0 +1,106 @@
+"""LES frames from files to the device (rsc_les_upload_async): the raw planes
+copied on the worker's copy stream and remapped by k_les_remap give the same
+scatterer state, bit for bit, as the oracle advancing on the frame that the
+numpy restatement of les.c reads, with the upload queued behind and ahead of
+advances that read the slot."""
+import numpy as np
+import pytest
+
+from oracle import les_oracle
+from simradar_gb300 import synth
+
+from test_gpu_parity import STATE_FIELDS, assert_state_equal, push_to_edges
+
+pytestmark = pytest.mark.gpu
+
+
+class Vol:
+    def __init__(self, uvwt, cpxx):
+        self.uvwt, self.cpxx = uvwt, cpxx
+
+
+def scene_and_folder(tmp_path, config, concept=synth.CONCEPT_DBU, frames=4):
+    cfg = synth.LESConfig(nx=96, ny=96, nz=48)
+    S = synth.make_scene(num_rain=30000, debris=[(synth.OBJ_LEAF, 512)], les_cfg=cfg, les_count=frames,
+                         concept=concept)
+    rng = np.random.default_rng(9)
+    for v in S.les:
+        v.cpxx[..., 0] = rng.uniform(-14.0, -12.0, v.cpxx.shape[:3])
+    push_to_edges(S)
+    d = str(tmp_path / config)
+    synth.write_les_folder(d, cfg, S.les, config=config)
+    return S, d
+
+
+def oracle_volume(d, config, n):
+    uvwt, cpxx, _ = les_oracle.frame(d, config, n)
+    return Vol(uvwt, cpxx)
+
+
+@pytest.mark.parametrize("config", ["suctvort", "flat"])
+def test_upload_matches_oracle(backend, oracle_lib, tmp_path, config):
+    concept = synth.CONCEPT_DBU if config == "suctvort" else synth.CONCEPT_FIXED_POS
+    S, d = scene_and_folder(tmp_path, config, concept)
+    src = backend.LESSource(d, config)
+    desc = src.descriptor()
+    assert np.array_equal(desc.view(np.uint32),
+                          les_oracle.descriptor(config, 96, 96, 48, *les_oracle.grid(d)[3:]).view(np.uint32))
+    S.les_desc = desc
+    pop = synth.population(S)
+    W = backend.Worker(0)
+    synth.load_worker(W, S, les_slot_volumes=())
+    t0 = src.upload_async(W, 0, 0)
+    assert t0 == 0.0
+    st = oracle_lib.OracleState(S.state)
+    vols = {0: oracle_volume(d, config, 0)}
+    slot_frame = {0: 0}
+    # (slot read by the advance, upload before it: (slot, frame) or None)
+    plan = [(0, (1, 1)), (0, None), (1, None), (1, (1, 2)), (1, (0, 3)), (0, None), (1, None)]
+    for k, (slot, up) in enumerate(plan):
+        if up is not None:
+            s_up, f_up = up
+            assert src.upload_async(W, s_up, f_up) == np.float32(f_up * float(S.les_cfg.tp))
+            slot_frame[s_up] = f_up
+            vols.setdefault(f_up, oracle_volume(d, config, f_up))
+        sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+        W.advance_time(pop, slot, sd)
+        W.make_pulse(sd)
+        oracle_lib.advance_time(st, S, S.counts, vols[slot_frame[slot]], sd)
+    assert_state_equal(W.download(STATE_FIELDS), st.s, where=config + " ")
+    W.close()
+    src.close()
+
+
+def test_upload_beside_set_les(backend, tmp_path):
+    """The same frames through rsc_les_upload_async and through rsc_set_les of
+    the host-remapped frame give the same state and pulses."""
+    S, d = scene_and_folder(tmp_path, "suctvort")
+    src = backend.LESSource(d, "suctvort")
+    S.les_desc = src.descriptor()
+    pop = synth.population(S)
+    A, B = backend.Worker(0), backend.Worker(0)
+    for W in (A, B):
+        synth.load_worker(W, S, les_slot_volumes=())
+    src.upload_async(A, 0, 0)
+    uvwt, cpxx, _ = src.read(0)
+    B.set_les(0, uvwt, cpxx, S.les_desc)
+    for k in range(8):
+        sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+        slot = (k // 2) % 2
+        if k % 2 == 1:
+            # refill the other slot while this one is in use
+            f = (k // 2 + 1) % 4
+            src.upload_async(A, 1 - slot, f)
+            uvwt, cpxx, _ = src.read(f)
+            B.set_les(1 - slot, uvwt, cpxx, S.les_desc)
+        for W in (A, B):
+            W.advance_time(pop, slot, sd)
+            W.make_pulse(sd)
+        # same state, same kernel: the pulses differ only by the order of
+        # the FP32 atomic additions
+        ga, gb = A.download_pulse(1.0), B.download_pulse(1.0)
+        np.testing.assert_allclose(ga, gb, rtol=1e-4, atol=1e-5 * float(np.abs(gb).max()), err_msg=str(k))
+    assert_state_equal(A.download(STATE_FIELDS), B.download(STATE_FIELDS))
+    A.close()
+    B.close()
+    src.close()
