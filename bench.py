@@ -30,6 +30,9 @@ Extra sections on one GPU (added to the same JSON line):
              compensated form: batched (two launches per step for all, CUDA
              graph, autotuned pulse shape) against the same instances run back
              to back one after another.
+  les        the LES frame swap inside the loop: no swap, the reference's
+             (host remap + blocking upload of uvwt / cpxx), and the frame
+             source (raw planes on the copy stream, remapped on the device).
   large      33,554,432 rain + 131,072 debris, LES 352x352x160, RHI
              0.5-20 deg at 0.02 deg, compensated form, I/Q streamed to pinned
              host buffers every 100 pulses and on to a .iq file by the
@@ -56,7 +59,7 @@ DEBRIS = ((1, 1024), (3, 1024), (6, 1024))
 GATES = 40
 METRIC = "pulses/s and scatterer-updates/s at 2M scatterers; HBM roofline frac; I/Q err vs FP64"
 UNIT = "pulses/s"
-SECTIONS = ("precision", "batch", "large")
+SECTIONS = ("precision", "batch", "les", "large")
 
 
 def workload_config(n_rain):
@@ -528,6 +531,73 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
             "iq_nonzero_pulses": int((np.abs(iq).sum(axis=(1, 2)) > 0).sum())}
 
 
+def bench_les(torch, rsc, synth, dev, S, steps=400, period=100):
+    """The LES frame swap inside the pulse loop (rs.c:5188-5200): every
+    `period` steps the next frame goes into the inactive slot and the loop
+    moves to it.  Three ways on the README workload: no swap; the reference's
+    (the frame already remapped on the host, as les.c's background thread
+    leaves it, then a blocking upload of uvwt + cpxx from pageable memory,
+    RS_set_vel_data); and the frame source (raw planes read ahead, copied on
+    the copy stream and remapped on the device, overlapped with the loop)."""
+    import shutil
+    import tempfile
+    tmpdir = tempfile.mkdtemp(prefix="simradar_les_")
+    frames = 4
+    synth.write_les_folder(tmpdir, S.les_cfg, [S.les[k % len(S.les)] for k in range(frames)])
+    src = rsc.LESSource(tmpdir, "suctvort")
+    pop = synth.population(S)
+    W = rsc.Worker(dev)
+    synth.load_worker(W, S)
+    stream = torch.cuda.ExternalStream(W.stream)
+    sd_seq = S.sd_seq
+    for k in range(3):
+        W.make_pulse(sd_seq[k])
+        W.advance_time(pop, 0, sd_seq[k])
+    W.synchronize()
+
+    def loop(mode):
+        slot, frame = 0, 0
+        upload_s = []
+        W.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            if mode != "none" and k % period == period - 1:
+                frame = (frame + 1) % frames
+                t1 = time.perf_counter()
+                if mode == "source":
+                    src.upload_async(W, 1 - slot, frame)
+                else:
+                    uvwt, cpxx = host_frames[frame]
+                    W.set_les(1 - slot, uvwt, cpxx, S.les_desc)
+                upload_s.append(time.perf_counter() - t1)
+            if mode != "none" and k % period == 0 and k > 0:
+                slot = 1 - slot
+            W.make_pulse(sd_seq[k % len(sd_seq)])
+            W.advance_time(pop, slot, sd_seq[k % len(sd_seq)])
+        W.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / steps, (statistics.mean(upload_s) * 1e3 if upload_s else 0.0)
+
+    # the reference's frames arrive remapped by les.c's background thread
+    host_frames = [src.read(f)[:2] for f in range(frames)]
+    loop("source")   # page the frames in, pin the source's buffers
+    none_ms, _ = loop("none")
+    ref_ms, ref_call = loop("blocking")
+    src_ms, src_call = loop("source")
+    W.close()
+    src.close()
+    shutil.rmtree(tmpdir, ignore_errors=True)
+    nn = S.les_cfg.nx * S.les_cfg.ny * S.les_cfg.nz
+    swaps = steps // period
+    return {"workload": "README loop (2M scatterers), LES %dx%dx%d, a frame swap every %d steps, %d steps"
+                        % (S.les_cfg.nx, S.les_cfg.ny, S.les_cfg.nz, period, steps),
+            "ms_per_step_no_swap": none_ms,
+            "ms_per_step_blocking_swap": ref_ms, "blocking_swap_call_ms": ref_call,
+            "ms_per_step_source_swap": src_ms, "source_swap_call_ms": src_call,
+            "swap_cost_ms_blocking": (ref_ms - none_ms) * steps / swaps,
+            "swap_cost_ms_source": (src_ms - none_ms) * steps / swaps,
+            "h2d_bytes_per_swap_blocking": nn * 32, "h2d_bytes_per_swap_source": nn * 20}
+
+
 def run_ours(args, rank, world):
     from simradar_gb300 import build as Bld
     from simradar_gb300 import rsc, synth
@@ -644,6 +714,8 @@ def run_ours(args, rank, world):
             extras["precision"] = bench_precision(torch, rsc, synth, dev, steps=min(args.steps, 50))
         if "batch" in wanted:
             extras["batch"] = bench_batch(torch, rsc, synth, dev, steps=40)
+        if "les" in wanted:
+            extras["les"] = bench_les(torch, rsc, synth, dev, S)
         if "large" in wanted:
             extras["large"] = bench_large(torch, rsc, synth, dev, chunks=4)
 

@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -109,6 +110,9 @@ struct rsc_worker {
     bool les_wait[2] = {false, false};
     float *les_raw = nullptr;
     size_t les_raw_n = 0;
+    /* uvwt of rsc_set_les on its way into a slot's x-pair layout */
+    float4 *les_stage = nullptr;
+    size_t les_stage_n = 0;
     Table2D adm[RSC_MAX_TYPES];
     Table2D rcs_tab[RSC_MAX_TYPES];
     float *dff[2] = {nullptr, nullptr};
@@ -246,6 +250,37 @@ Image make_image(const float4 *d, uint32_t nx, uint32_t ny, uint32_t nz) {
     im.ny = (int)ny;
     im.nz = (int)nz;
     return im;
+}
+
+rsc::PairImage make_pair_image(const float4 *d, uint32_t nx, uint32_t ny, uint32_t nz) {
+    rsc::PairImage im;
+    im.data = d;
+    im.nx = (int)nx;
+    im.ny = (int)ny;
+    im.nz = (int)nz;
+    return im;
+}
+
+/* float4 count of an LES uvwt slot in x-pair layout */
+size_t les_pair_float4s(uint32_t nx, uint32_t ny, uint32_t nz) { return 2 * ((size_t)nx + 2) * ny * nz; }
+
+/* Grid of the LES layout kernels for nx x rows. */
+dim3 les_grid(uint32_t nx, size_t rows) {
+    return dim3((unsigned)((nx + 2 + rsc::kLesThreads - 1) / rsc::kLesThreads), (unsigned)std::min<size_t>(rows, 65535));
+}
+
+/* A device array of at least n elements (contents not kept). */
+template <typename T>
+int ensure_buffer(T **p, size_t *cap, size_t n, cudaStream_t wait_stream) {
+    if (*cap >= n) return RSC_OK;
+    if (wait_stream) cudaStreamSynchronize(wait_stream);
+    free_ptr(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(RSC_ERR_NOMEM, "%zu MB of LES staging: %s", (n * sizeof(T)) >> 20, cudaGetErrorString(e));
+    *cap = n;
+    return RSC_OK;
 }
 
 /* Debris launch description shared by the advance kernels and k_db_rcs. */
@@ -525,6 +560,7 @@ int rsc_worker_free(rsc_worker *w) {
         cudaStreamDestroy(w->les_copy);
     }
     free_ptr(w->les_raw);
+    free_ptr(w->les_stage);
     if (w->les_mark) cudaEventDestroy(w->les_mark);
     for (int s = 0; s < 2; s++) {
         if (w->les_ready[s]) cudaEventDestroy(w->les_ready[s]);
@@ -650,7 +686,9 @@ static int les_slot_wait(rsc_worker *w, int slot) {
 /* Both LES slots allocated for nx x ny x nz texels. */
 static int ensure_les_slots(rsc_worker *w, uint32_t nx, uint32_t ny, uint32_t nz) {
     const size_t nn = (size_t)nx * ny * nz;
-    if (nn >= (1ull << 31)) return fail(RSC_ERR_UNSUPPORTED, "LES of %zu texels (the kernels index below 2^31)", nn);
+    if (((size_t)nx + 2) * ny * nz >= (1ull << 31)) {
+        return fail(RSC_ERR_UNSUPPORTED, "LES of %zu texels (the kernels index below 2^31)", nn);
+    }
     if (w->les_uvwt[0] != nullptr && (nx != w->les_nx || ny != w->les_ny || nz != w->les_nz)) {
         /* new dimensions: reallocate both slots (rs.c:3000-3016 releases them) */
         cudaStreamSynchronize(w->stream);
@@ -664,7 +702,7 @@ static int ensure_les_slots(rsc_worker *w, uint32_t nx, uint32_t ny, uint32_t nz
     }
     if (w->les_uvwt[0] == nullptr) {
         for (int k = 0; k < 2; k++) {
-            RSC_CUDA(cudaMalloc((void **)&w->les_uvwt[k], nn * sizeof(float4)));
+            RSC_CUDA(cudaMalloc((void **)&w->les_uvwt[k], les_pair_float4s(nx, ny, nz) * sizeof(float4)));
             RSC_CUDA(cudaMalloc((void **)&w->les_cpxx[k], nn * sizeof(float4)));
             RSC_CUDA(cudaMemsetAsync(w->les_cpxx[k], 0, nn * sizeof(float4), w->stream));
         }
@@ -688,7 +726,13 @@ static int set_les_impl(rsc_worker *w, int slot, const float *uvwt4, const float
     s = les_slot_wait(w, slot);
     if (s) return s;
     const size_t nn = (size_t)nx * ny * nz;
-    RSC_CUDA(cudaMemcpyAsync(w->les_uvwt[slot], uvwt4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
+    s = ensure_buffer(&w->les_stage, &w->les_stage_n, nn, w->stream);
+    if (s) return s;
+    RSC_CUDA(cudaMemcpyAsync(w->les_stage, uvwt4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
+    rsc::k_les_pairs<<<les_grid(nx, (size_t)ny * nz), rsc::kLesThreads, 0, w->stream>>>(w->les_stage, (int)nx,
+                                                                                      (size_t)ny * nz, w->les_uvwt[slot]);
+    RSC_CUDA(cudaGetLastError());
+    w->launches++;
     if (cpxx4) {
         RSC_CUDA(cudaMemcpyAsync(w->les_cpxx[slot], cpxx4, nn * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
     }
@@ -724,16 +768,9 @@ int rsc_les_upload_async(rsc_worker *w, rsc_les_source *src, int slot, uint32_t 
         RSC_CUDA(cudaEventCreateWithFlags(&w->les_mark, cudaEventDisableTiming));
         for (int k = 0; k < 2; k++) RSC_CUDA(cudaEventCreateWithFlags(&w->les_ready[k], cudaEventDisableTiming));
     }
-    if (w->les_raw_n != 5 * nn) {
-        /* the staging buffer is reused in copy-stream order */
-        RSC_CUDA(cudaStreamSynchronize(w->les_copy));
-        free_ptr(w->les_raw);
-        w->les_raw = nullptr;
-        w->les_raw_n = 0;
-        cudaError_t e = cudaMalloc((void **)&w->les_raw, 5 * nn * sizeof(float));
-        if (e != cudaSuccess) return cuda_fail(RSC_ERR_NOMEM, "LES staging of %zu MB: %s", 5 * nn * 4 >> 20, cudaGetErrorString(e));
-        w->les_raw_n = 5 * nn;
-    }
+    /* the staging buffer is reused in copy-stream order */
+    s = ensure_buffer(&w->les_raw, &w->les_raw_n, 5 * nn, w->les_copy);
+    if (s) return s;
     rscles::Held h;
     const char *why = "";
     s = rscles::acquire(src, frame, &h, &why);
@@ -747,9 +784,9 @@ int rsc_les_upload_async(rsc_worker *w, rsc_les_source *src, int slot, uint32_t 
     /* the slot is rewritten after the work queued on the worker so far */
     RSC_CUDA(cudaEventRecord(w->les_mark, w->stream));
     RSC_CUDA(cudaStreamWaitEvent(w->les_copy, w->les_mark, 0));
-    const int grid = w->num_sms * 8;
-    rsc::k_les_remap<<<grid, 256, 0, w->les_copy>>>(w->les_raw, nn, I.v0, I.p0, I.t0, I.p_for_cn2, w->les_uvwt[slot],
-                                                    w->les_cpxx[slot]);
+    const size_t rows = (size_t)I.ny * I.nz;
+    rsc::k_les_remap<<<les_grid(I.nx, rows), rsc::kLesThreads, 0, w->les_copy>>>(
+        w->les_raw, (int)I.nx, rows, I.v0, I.p0, I.t0, I.p_for_cn2, w->les_uvwt[slot], w->les_cpxx[slot]);
     RSC_CUDA(cudaGetLastError());
     RSC_CUDA(cudaEventRecord(w->les_ready[slot], w->les_copy));
     w->les_wait[slot] = true;
@@ -1155,7 +1192,7 @@ static int fill_advance_args(rsc_worker *w, const rsc_population *pop, int les_i
     a.tum = w->tum;
     a.rcs = w->rcs;
     a.rnd = w->rnd;
-    a.uvwt = make_image(w->les_uvwt[les_id], w->les_nx, w->les_ny, w->les_nz);
+    a.uvwt = make_pair_image(w->les_uvwt[les_id], w->les_nx, w->les_ny, w->les_nz);
     a.cpxx = make_image(w->les_cpxx[les_id], w->les_nx, w->les_ny, w->les_nz);
     memcpy(a.wind, w->les_desc, sizeof(a.wind));
     memcpy(a.sim, sim_desc, sizeof(a.sim));
@@ -1403,6 +1440,8 @@ struct rsc_batch {
      * last run that read the slot, the event of the refill's completion and
      * whether a run still has to wait for it */
     cudaStream_t copy_stream = nullptr;
+    float4 *les_stage = nullptr;   /* uvwt of rsc_batch_set_les_async before its pair layout */
+    size_t les_stage_n = 0;
     std::vector<cudaEvent_t> slot_used, slot_ready;
     std::vector<char> slot_pending;
 };
@@ -1481,7 +1520,7 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
             return fail(s, "instance %zu: %s", i, why);
         }
         for (int slot = 0; slot < 2; slot++) {
-            A.uvwt[slot] = make_image(x->les_uvwt[slot], x->les_nx, x->les_ny, x->les_nz);
+            A.uvwt[slot] = make_pair_image(x->les_uvwt[slot], x->les_nx, x->les_ny, x->les_nz);
             A.cpxx[slot] = make_image(x->les_cpxx[slot], x->les_nx, x->les_ny, x->les_nz);
             A.dff[slot] = x->dff[slot];
         }
@@ -1724,6 +1763,7 @@ int rsc_batch_free(rsc_batch *b) {
     free_ptr(b->d_adv_prefix);
     free_ptr(b->d_pulse_prefix);
     if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
+    free_ptr(b->les_stage);
     for (cudaEvent_t ev : b->slot_used) {
         if (ev) cudaEventDestroy(ev);
     }
@@ -1914,12 +1954,19 @@ int rsc_batch_set_les_async(rsc_batch *b, int index, int slot, const float *uvwt
         return fail(RSC_ERR_STATE, "instance %d: LES of %ux%ux%u not set with rsc_set_les", index, nx, ny, nz);
     }
     const size_t q = 2 * (size_t)index + slot;
-    const size_t bytes = (size_t)nx * ny * nz * sizeof(float4);
-    /* after the last batch run and any worker-stream work that read the slot */
+    const size_t nn = (size_t)nx * ny * nz, bytes = nn * sizeof(float4);
+    /* uvwt to the batch's staging buffer (reused in copy-stream order) */
+    s = ensure_buffer(&b->les_stage, &b->les_stage_n, nn, b->copy_stream);
+    if (s) return s;
+    RSC_CUDA(cudaMemcpyAsync(b->les_stage, uvwt4, bytes, cudaMemcpyHostToDevice, b->copy_stream));
+    /* the slot changes after the last batch run and any worker-stream work that read it */
     RSC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->slot_used[q], 0));
     RSC_CUDA(cudaEventRecord(b->ev_join, x->stream));
     RSC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->ev_join, 0));
-    RSC_CUDA(cudaMemcpyAsync(x->les_uvwt[slot], uvwt4, bytes, cudaMemcpyHostToDevice, b->copy_stream));
+    rsc::k_les_pairs<<<les_grid(nx, (size_t)ny * nz), rsc::kLesThreads, 0, b->copy_stream>>>(
+        b->les_stage, (int)nx, (size_t)ny * nz, x->les_uvwt[slot]);
+    RSC_CUDA(cudaGetLastError());
+    b->launches++;
     if (cpxx4) RSC_CUDA(cudaMemcpyAsync(x->les_cpxx[slot], cpxx4, bytes, cudaMemcpyHostToDevice, b->copy_stream));
     RSC_CUDA(cudaEventRecord(b->slot_ready[q], b->copy_stream));
     b->slot_pending[q] = 1;

@@ -30,7 +30,8 @@ struct BatchStep {
  * debris-flux-field slots (the step picks one) */
 struct BatchAdvance {
     AdvanceArgs a;
-    Image uvwt[2], cpxx[2];
+    PairImage uvwt[2];
+    Image cpxx[2];
     const float *dff[2];
 };
 

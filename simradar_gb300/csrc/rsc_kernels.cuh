@@ -10,6 +10,7 @@
  *   k_sig_aux     forms aux / sig for RS_download when the pulse kernel did
  *                 not write them.
  *   k_les_remap   scales an LES frame's raw planes into a uvwt / cpxx slot.
+ *   k_les_pairs   puts a uvwt volume into the slot's x-pair layout.
  * plus the pieces the pulse kernel (rsc_pulse.cuh) is built from: the
  * pass-1 weights, the per-scatterer signal and the per-warp gate bins.
  */
@@ -33,7 +34,8 @@ struct DebrisType {
 struct AdvanceArgs {
     float4 *pos, *vel, *ori, *tum, *rcs;
     uint4 *rnd;
-    Image uvwt, cpxx;
+    PairImage uvwt;
+    Image cpxx;
     float wind[16];
     float sim[16];
     const float4 *drop;
@@ -154,7 +156,7 @@ __device__ __forceinline__ void rain_fp(const AdvanceArgs &a, size_t i, float4 &
     float4 rcs = a.rcs[i];
     float c3[3];
     wind_table_index(c3, pos, a.wind, sd);
-    float4 uv = read_image3d(a.uvwt, c3[0], c3[1], c3[2]);
+    float4 uv = read_pair_image3d(a.uvwt, c3[0], c3[1], c3[2]);
     float4 cp = read_image3d(a.cpxx, c3[0], c3[1], c3[2]);
     float l = len3(pos.x, pos.y, pos.z);
     float nx = pos.x / l, ny = pos.y / l, nz = pos.z / l;
@@ -622,20 +624,47 @@ __global__ void __launch_bounds__(256) k_sig_aux(const PulseArgs P) {
     P.sig[i] = make_float4(sg.sig[0], sg.sig[1], sg.sig[2], sg.sig[3]);
 }
 
+/* Launch shape of the LES layout kernels: blockIdx.x * 128 + threadIdx.x =
+ * pair q in [0, nx + 2), rows (j, k) of the volume from blockIdx.y in steps
+ * of gridDim.y. */
+constexpr int kLesThreads = 128;
+
 /* The remap of an LES frame (les.c:388-406): the file's u, v, w, p, t
- * planes (nn floats each) scaled into uvwt = (u v0, v v0, w v0, t t0) and
- * cpxx = (0, p p0, 0, 0), or (p p0, 0, 0, 0) when p is the cn2 of the flat
- * configuration.  Reads 20 B and writes 32 B per cell, coalesced. */
-__global__ void __launch_bounds__(256) k_les_remap(const float *__restrict__ raw, size_t nn, float v0, float p0,
-                                                   float t0, int p_for_cn2, float4 *__restrict__ uvwt,
-                                                   float4 *__restrict__ cpxx) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += stride) {
-        const float u = __ldg(raw + k), v = __ldg(raw + nn + k), w = __ldg(raw + 2 * nn + k);
-        const float p = __ldg(raw + 3 * nn + k), t = __ldg(raw + 4 * nn + k);
-        uvwt[k] = make_float4(u * v0, v * v0, w * v0, t * t0);
-        const float pp = p * p0;
-        cpxx[k] = p_for_cn2 ? make_float4(pp, 0.0f, 0.0f, 0.0f) : make_float4(0.0f, pp, 0.0f, 0.0f);
+ * planes (nn floats each) scaled into uvwt = (u v0, v v0, w v0, t t0), stored
+ * in x-pair layout, and cpxx = (0, p p0, 0, 0), or (p p0, 0, 0, 0) when p is
+ * the cn2 of the flat configuration. */
+__global__ void __launch_bounds__(kLesThreads) k_les_remap(const float *__restrict__ raw, int nx, size_t rows,
+                                                           float v0, float p0, float t0, int p_for_cn2,
+                                                           float4 *__restrict__ uvwt, float4 *__restrict__ cpxx) {
+    const int q = blockIdx.x * kLesThreads + threadIdx.x;
+    if (q >= nx + 2) return;
+    const size_t nn = rows * nx;
+    for (size_t row = blockIdx.y; row < rows; row += gridDim.y) {
+        const size_t k0 = row * nx + (size_t)min(max(q - 1, 0), nx - 1), k1 = row * nx + (size_t)min(q, nx - 1);
+        const float4 a = make_float4(__ldg(raw + k0) * v0, __ldg(raw + nn + k0) * v0, __ldg(raw + 2 * nn + k0) * v0,
+                                     __ldg(raw + 4 * nn + k0) * t0);
+        const float4 b = make_float4(__ldg(raw + k1) * v0, __ldg(raw + nn + k1) * v0, __ldg(raw + 2 * nn + k1) * v0,
+                                     __ldg(raw + 4 * nn + k1) * t0);
+        float4 *o = uvwt + 2 * (row * (size_t)(nx + 2) + q);
+        o[0] = a;
+        o[1] = b;
+        if (q >= 1 && q <= nx) {
+            const size_t k = row * nx + (q - 1);
+            const float pp = __ldg(raw + 3 * nn + k) * p0;
+            cpxx[k] = p_for_cn2 ? make_float4(pp, 0.0f, 0.0f, 0.0f) : make_float4(0.0f, pp, 0.0f, 0.0f);
+        }
+    }
+}
+
+/* uvwt (rows * nx float4, x fastest) into the x-pair layout */
+__global__ void __launch_bounds__(kLesThreads) k_les_pairs(const float4 *__restrict__ src, int nx, size_t rows,
+                                                           float4 *__restrict__ uvwt) {
+    const int q = blockIdx.x * kLesThreads + threadIdx.x;
+    if (q >= nx + 2) return;
+    for (size_t row = blockIdx.y; row < rows; row += gridDim.y) {
+        float4 *o = uvwt + 2 * (row * (size_t)(nx + 2) + q);
+        o[0] = __ldg(src + row * nx + min(max(q - 1, 0), nx - 1));
+        o[1] = __ldg(src + row * nx + min(q, nx - 1));
     }
 }
 

@@ -5,7 +5,8 @@
  * fmaf appears exactly where rs.cl writes fma), with the elementary functions
  * of rsmath.h.  Texture reads are software filters over float4 arrays in HBM
  * (L2-resident), because the texture unit's 8-bit filter weights would not
- * reproduce OpenCL's single-precision linear filter.
+ * reproduce OpenCL's single-precision linear filter; the LES wind volume is
+ * kept in an x-pair layout so that the filter reads it in four 32-byte loads.
  */
 #ifndef SIMRADAR_GB300_RSC_PHYSICS_CUH
 #define SIMRADAR_GB300_RSC_PHYSICS_CUH
@@ -128,6 +129,50 @@ __device__ __forceinline__ float4 read_image3d(const Image &im, float u, float v
     return r;
 }
 
+/* The LES wind volume (uvwt) in x-pair layout: every row (j, k) holds nx + 2
+ * pairs of texels, pair q = (T[clamp(q - 1)], T[clamp(q)]) with the clamp to
+ * [0, nx - 1], 32 bytes each.  The linear filter's x axis reads texels
+ * i0 = clamp(i) and i1 = clamp(i + 1) for i = floor(u - 0.5) in [-1, nx]:
+ * both are pair i + 1, one 32-byte aligned load instead of two gathers. */
+struct PairImage {
+    const float4 *data;   /* 2 * (nx + 2) * ny * nz float4 */
+    int nx, ny, nz;
+};
+
+/* one 32-byte load of two texels (the pointer is 32-byte aligned) */
+__device__ __forceinline__ void ldg_pair(const float4 *p, float4 &a, float4 &b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
+/* read_image3d on the x-pair layout: the same texels, weights and sums */
+__device__ __forceinline__ float4 read_pair_image3d(const PairImage &im, float u, float v, float w) {
+    int j0, j1, k0, k1;
+    float b, c;
+    tex_axis(v, im.ny, &j0, &j1, &b);
+    tex_axis(w, im.nz, &k0, &k1, &c);
+    const float uu = u - 0.5f;
+    const float fl = floorf(uu);
+    const float a = uu - fl;
+    const unsigned q = (unsigned)((int)fminf(fmaxf(fl, -1.0f), (float)im.nx) + 1);
+    const unsigned sy = (unsigned)im.nx + 2u, sz = sy * (unsigned)im.ny;
+    const float4 *d = im.data;
+    float4 t000, t100, t010, t110, t001, t101, t011, t111;
+    ldg_pair(d + 2 * (size_t)(j0 * sy + k0 * sz + q), t000, t100);
+    ldg_pair(d + 2 * (size_t)(j1 * sy + k0 * sz + q), t010, t110);
+    ldg_pair(d + 2 * (size_t)(j0 * sy + k1 * sz + q), t001, t101);
+    ldg_pair(d + 2 * (size_t)(j1 * sy + k1 * sz + q), t011, t111);
+    float ma = 1.0f - a, mb = 1.0f - b, mc = 1.0f - c;
+    float w000 = ma * mb * mc, w100 = a * mb * mc, w010 = ma * b * mc, w110 = a * b * mc;
+    float w001 = ma * mb * c, w101 = a * mb * c, w011 = ma * b * c, w111 = a * b * c;
+#define RSC_TRI(L) (w000 * t000.L + w100 * t100.L + w010 * t010.L + w110 * t110.L + \
+                    w001 * t001.L + w101 * t101.L + w011 * t011.L + w111 * t111.L)
+    float4 r = f4(RSC_TRI(x), RSC_TRI(y), RSC_TRI(z), RSC_TRI(w));
+#undef RSC_TRI
+    return r;
+}
+
 /* read_imagef on an image2d_t */
 __device__ __forceinline__ float4 read_image2d(const Image &im, float u, float v) {
     int i0, i1, j0, j1;
@@ -166,10 +211,10 @@ __device__ __forceinline__ void wind_table_index(float out[3], float4 pos, const
     }
 }
 
-__device__ __forceinline__ float4 compute_bg_vel(float4 pos, const Image &uvwt, const float *wd, const float *sd) {
+__device__ __forceinline__ float4 compute_bg_vel(float4 pos, const PairImage &uvwt, const float *wd, const float *sd) {
     float c[3];
     wind_table_index(c, pos, wd, sd);
-    return read_image3d(uvwt, c[0], c[1], c[2]);
+    return read_pair_image3d(uvwt, c[0], c[1], c[2]);
 }
 
 /* compute_dudt_dwdt (rs.cl:195-261) */
