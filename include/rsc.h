@@ -134,8 +134,9 @@ int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float 
 
 /* One time step of every scatterer: the el_atts / bg_atts / fp_atts launch on
  * type 0 (chosen by the concept bits in sim_desc[5], rs.c:5339-5349) and the
- * db_atts launch for each debris type (rs.c:5350-5374), in one kernel launch,
- * reading LES slot les_id.  Replaces the launches and the wait of
+ * db_atts launch for each debris type (rs.c:5350-5374), as two kernels: the
+ * background range, and every debris range together beside it on a
+ * high-priority stream, reading LES slot les_id.  Replaces the launches and the wait of
  * RS_advance_time (rs.c:5325-5388).  Asynchronous unless the caller
  * synchronises; rsc_download / rsc_download_pulse synchronise. */
 int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const float sim_desc[16]);
@@ -157,11 +158,12 @@ int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain);
 /* Wait for all work queued on the worker (clFinish). */
 int rsc_synchronize(rsc_worker *w);
 
-/* The latest pulse copied to pulse4 (range_count float4, no gain) in the
- * worker's stream order, without waiting: the copy is complete after
- * rsc_synchronize.  With page-locked pulse4 the host can queue the next
- * pulses while earlier copies are in flight (additive; the reference reads
- * each pulse with a blocking clEnqueueReadBuffer, rs.c:5115). */
+/* The latest pulse copied to pulse4 (range_count float4, no gain) without
+ * waiting: the copy runs on a stream of its own once the pulse is formed, so
+ * the next advance does not wait for it (the next pulse does), and it is
+ * complete after rsc_synchronize.  With page-locked pulse4 the host can queue
+ * the next pulses while earlier copies are in flight (additive; the
+ * reference reads each pulse with a blocking clEnqueueReadBuffer, rs.c:5115). */
 int rsc_download_pulse_async(rsc_worker *w, float *pulse4);
 
 /* Pulse-formation precision, RSC_PULSE_* (additive, default PLAIN). */

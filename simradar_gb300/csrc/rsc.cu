@@ -141,6 +141,12 @@ struct rsc_worker {
      * that reads or changes the state or the tables runs it alone first */
     int fuse = 0;
     cudaStream_t side = nullptr;             /* debris kernel beside the background kernel */
+    /* rsc_download_pulse_async: the pulse goes to the host on its own stream,
+     * so the next advance does not wait for the copy; the next pulse kernel
+     * (which rewrites the pulse) waits for d2h_done */
+    cudaStream_t d2h = nullptr;
+    cudaEvent_t pulse_ev = nullptr, d2h_done = nullptr;
+    bool d2h_pending = false;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     bool pend = false;
     AdvanceArgs pend_a;
@@ -200,6 +206,8 @@ void attribute_arrays(rsc_worker *w, uint4 **out[8]) {
 }
 
 void free_arrays(rsc_worker *w) {
+    if (w->d2h) cudaStreamSynchronize(w->d2h);
+    w->d2h_pending = false;
     free_ptr(w->pos);
     free_ptr(w->vel);
     free_ptr(w->ori);
@@ -524,7 +532,11 @@ int rsc_worker_create(int device, rsc_worker **out) {
     w->device = device;
     cudaError_t e = cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->side, cudaStreamNonBlocking);
+    /* the debris kernel's few blocks take SM slots ahead of the background
+     * kernel's queued blocks, so they run beside it rather than after it */
+    int prio_least = 0, prio_greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&w->side, cudaStreamNonBlocking, prio_greatest);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->join_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -569,6 +581,12 @@ int rsc_worker_free(rsc_worker *w) {
         cudaStreamSynchronize(w->side);
         cudaStreamDestroy(w->side);
     }
+    if (w->d2h) {
+        cudaStreamSynchronize(w->d2h);
+        cudaStreamDestroy(w->d2h);
+    }
+    if (w->pulse_ev) cudaEventDestroy(w->pulse_ev);
+    if (w->d2h_done) cudaEventDestroy(w->d2h_done);
     if (w->fork_ev) cudaEventDestroy(w->fork_ev);
     if (w->join_ev) cudaEventDestroy(w->join_ev);
     if (w->stream) cudaStreamDestroy(w->stream);
@@ -672,6 +690,15 @@ int rsc_set_rcs_ellipsoid(rsc_worker *w, const float *table4, uint32_t n, const 
     if (s) return s;
     w->ellipsoid_n = n;
     memcpy(w->ellipsoid_desc, desc, sizeof(w->ellipsoid_desc));
+    return RSC_OK;
+}
+
+/* The worker's stream waits for an asynchronous pulse copy before the pulse
+ * is rewritten. */
+static int pulse_d2h_wait(rsc_worker *w) {
+    if (!w->d2h_pending) return RSC_OK;
+    RSC_CUDA(cudaStreamWaitEvent(w->stream, w->d2h_done, 0));
+    w->d2h_pending = false;
     return RSC_OK;
 }
 
@@ -1292,6 +1319,8 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     size_t smem = 0;
     s = pulse_geometry(w, mode, pulse_path(P), &grid, &threads, &smem);
     if (s) return s;
+    s = pulse_d2h_wait(w);
+    if (s) return s;
     const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
     P.materialize = mat ? 1 : 0;
     if (w->pend && mode != RSC_PULSE_F64) {
@@ -1338,10 +1367,22 @@ int rsc_download_pulse(rsc_worker *w, float *pulse4, float gain) {
 int rsc_download_pulse_async(rsc_worker *w, float *pulse4) {
     int s = check_alloc(w);
     if (s) return s;
+    s = flush_pending(w);
+    if (s) return s;
     if (pulse4 == nullptr) return fail(RSC_ERR_ARG, "pulse4 is NULL");
-    RSC_CUDA(cudaMemcpyAsync(pulse4, w->pulse, w->G * sizeof(float4), cudaMemcpyDeviceToHost, w->stream));
+    if (w->d2h == nullptr) {
+        RSC_CUDA(cudaStreamCreateWithFlags(&w->d2h, cudaStreamNonBlocking));
+        RSC_CUDA(cudaEventCreateWithFlags(&w->pulse_ev, cudaEventDisableTiming));
+        RSC_CUDA(cudaEventCreateWithFlags(&w->d2h_done, cudaEventDisableTiming));
+    }
+    RSC_CUDA(cudaEventRecord(w->pulse_ev, w->stream));
+    RSC_CUDA(cudaStreamWaitEvent(w->d2h, w->pulse_ev, 0));
+    RSC_CUDA(cudaMemcpyAsync(pulse4, w->pulse, w->G * sizeof(float4), cudaMemcpyDeviceToHost, w->d2h));
+    RSC_CUDA(cudaEventRecord(w->d2h_done, w->d2h));
+    w->d2h_pending = true;
     return RSC_OK;
 }
+
 
 int rsc_synchronize(rsc_worker *w) {
     int s = check_worker(w);
@@ -1349,6 +1390,8 @@ int rsc_synchronize(rsc_worker *w) {
     s = flush_pending(w);
     if (s) return s;
     RSC_CUDA(cudaStreamSynchronize(w->stream));
+    if (w->d2h) RSC_CUDA(cudaStreamSynchronize(w->d2h));
+    w->d2h_pending = false;
     return RSC_OK;
 }
 
@@ -1669,6 +1712,8 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
     fill_pulse_args(w, P, sim_desc);
     if (mode == RSC_PULSE_COMPENSATED) P.rk = w->rk_hi;
     P.materialize = 0;
+    s = pulse_d2h_wait(w);
+    if (s) return s;
     EventPair ev;
     RSC_CUDA(ev.init());
     float best = INFINITY;

@@ -346,6 +346,37 @@ def test_download_pulse_async(backend, scene_db):
     W.close()
 
 
+def test_download_pulse_async_queued(backend, scene_db):
+    """Pulses copied asynchronously into page-locked buffers while the host
+    queues the following steps: each buffer holds its own step's pulse (the
+    next pulse kernel waits for the copy), compared with a second worker that
+    reads every pulse with a blocking download."""
+    torch = pytest.importorskip("torch")
+    S = scene_db
+    pop = synth.population(S)
+    A, B = backend.Worker(0), backend.Worker(0)
+    for W in (A, B):
+        synth.load_worker(W, S)
+    K = 8
+    ring = torch.empty((K, S.range_count, 4), dtype=torch.float32).pin_memory().numpy()
+    refs = []
+    for k in range(K):
+        sd = synth.pulse_sim_desc(S, 5 * k)
+        A.make_pulse(sd)
+        A.download_pulse_async(ring[k])
+        A.advance_time(pop, 0, sd)
+        B.make_pulse(sd)
+        refs.append(B.download_pulse(1.0))
+        B.advance_time(pop, 0, sd)
+    A.synchronize()
+    for k in range(K):
+        scale = float(np.abs(refs[k]).max())
+        assert scale > 0.0
+        np.testing.assert_allclose(ring[k], refs[k], rtol=1e-4, atol=1e-5 * scale, err_msg=str(k))
+    A.close()
+    B.close()
+
+
 @pytest.mark.parametrize("precision", [0, 1, 2])
 def test_max_gates(backend, oracle_lib, precision):
     """RSC_MAX_GATES (512) gates: the largest shared-memory bins of every
