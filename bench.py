@@ -27,7 +27,7 @@ Extra sections on one GPU (added to the same JSON line):
              series) and the throughput of each form.
   batch      64 instances (scatterers log-uniform 65,536-4,194,304, debris
              0-4096 per type, N0 4000-16000, PPI / RHI mix) in the
-             compensated form: batched (two launches per step for all, CUDA
+             compensated form: batched (three launches per step for all, CUDA
              graph, autotuned pulse shape) against the same instances run back
              to back one after another.
   les        the LES frame swap inside the loop: no swap, the reference's

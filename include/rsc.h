@@ -215,9 +215,10 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
 /* ---- batching form (additive; no counterpart in rs.c) ----
  * A batch runs many emulation instances -- each an rsc_worker with its own
  * state, tables, gates, concept and population, all on one device -- one
- * time step at a time, with two launches per step for all of them (pulse,
- * then advance, the order of simradar's loop, simradar.c:1032-1070).  Each
- * instance evolves exactly as it would alone. */
+ * time step at a time, with three launches per step for all of them (the
+ * pulse, then the background advance and, beside it on a high-priority
+ * stream, the debris advance: the order of simradar's loop,
+ * simradar.c:1032-1070).  Each instance evolves exactly as it would alone. */
 typedef struct rsc_batch rsc_batch;
 
 /* The workers must be allocated and have their tables set.  The batch keeps
@@ -268,8 +269,9 @@ int rsc_batch_set_les_async(rsc_batch *b, int index, int slot, const float *uvwt
                             uint32_t ny, uint32_t nz);
 /* The largest gate count of the batch (the row length of pulses_out). */
 int rsc_batch_max_gates(rsc_batch *b, int *max_gates);
-/* Kernel launches the batch has issued (2 per step with scatterers to
- * advance, plus the autotuner's). */
+/* Kernel launches the batch has issued (per step the pulse, plus the
+ * background and the debris advance where the batch has such scatterers,
+ * plus the autotuner's). */
 int rsc_batch_launch_count(rsc_batch *b, uint64_t *count);
 /* The CUDA stream the batch issues on. */
 int rsc_batch_get_stream(rsc_batch *b, void **stream);

@@ -1454,6 +1454,9 @@ struct rsc_batch {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_join = nullptr, ev_h2d = nullptr, ev_done = nullptr;
+    /* the debris kernel beside the background kernel (high priority) */
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, side_ev = nullptr;
     std::vector<rsc_worker *> w;
     std::vector<rsc_population> pops;
     bool have_pops = false;
@@ -1463,12 +1466,12 @@ struct rsc_batch {
     /* per-instance launch descriptors and block prefixes */
     std::vector<rsc::BatchAdvance> h_adv;
     std::vector<PulseArgs> h_pulse;
-    std::vector<unsigned> h_adv_prefix, h_pulse_prefix;
+    std::vector<unsigned> h_rain_prefix, h_deb_prefix, h_pulse_prefix;
     std::vector<uint32_t> concept;
     rsc::BatchAdvance *d_adv = nullptr;
     PulseArgs *d_pulse = nullptr;
-    unsigned *d_adv_prefix = nullptr, *d_pulse_prefix = nullptr;
-    unsigned adv_blocks = 0, pulse_blocks = 0;
+    unsigned *d_rain_prefix = nullptr, *d_deb_prefix = nullptr, *d_pulse_prefix = nullptr;
+    unsigned rain_blocks = 0, deb_blocks = 0, pulse_blocks = 0;
     int pulse_threads = 0, pulse_per_sm = 0;
     size_t pulse_smem = 0;
     /* per-step descriptors (pinned on the host) and the pulses of a run */
@@ -1543,10 +1546,11 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
     for (rsc_worker *x : b->w) sum_n += (double)x->num_scats;
     b->h_adv.assign(n, rsc::BatchAdvance());
     b->h_pulse.assign(n, PulseArgs());
-    b->h_adv_prefix.assign(n + 1, 0u);
+    b->h_rain_prefix.assign(n + 1, 0u);
+    b->h_deb_prefix.assign(n + 1, 0u);
     b->h_pulse_prefix.assign(n + 1, 0u);
     b->concept.assign(n, 0u);
-    unsigned acc_a = 0, acc_p = 0;
+    unsigned acc_r = 0, acc_d = 0, acc_p = 0;
     for (size_t i = 0; i < n; i++) {
         rsc_worker *x = b->w[i];
         if (x->pos == nullptr) return fail(RSC_ERR_STATE, "instance %zu is not allocated", i);
@@ -1567,8 +1571,10 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
             A.cpxx[slot] = make_image(x->les_cpxx[slot], x->les_nx, x->les_ny, x->les_nz);
             A.dff[slot] = x->dff[slot];
         }
-        b->h_adv_prefix[i] = acc_a;
-        acc_a += blocks;
+        b->h_rain_prefix[i] = acc_r;
+        acc_r += A.a.rain_blocks;
+        b->h_deb_prefix[i] = acc_d;
+        acc_d += blocks - A.a.rain_blocks;
         PulseArgs &P = b->h_pulse[i];
         fill_pulse_args(x, P, row[i].sim);
         if (b->mode == RSC_PULSE_COMPENSATED) P.rk = x->rk_hi;
@@ -1584,12 +1590,15 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
         acc_p += bi;
         b->concept[i] = rsm_f2u(row[i].sim[5]);
     }
-    b->h_adv_prefix[n] = acc_a;
+    b->h_rain_prefix[n] = acc_r;
+    b->h_deb_prefix[n] = acc_d;
     b->h_pulse_prefix[n] = acc_p;
-    if (acc_a != b->adv_blocks || acc_p != b->pulse_blocks || threads != b->pulse_threads || smem != b->pulse_smem) {
+    if (acc_r != b->rain_blocks || acc_d != b->deb_blocks || acc_p != b->pulse_blocks || threads != b->pulse_threads ||
+        smem != b->pulse_smem) {
         batch_drop_graph(b);
     }
-    b->adv_blocks = acc_a;
+    b->rain_blocks = acc_r;
+    b->deb_blocks = acc_d;
     b->pulse_blocks = acc_p;
     b->pulse_threads = threads;
     b->pulse_smem = smem;
@@ -1597,8 +1606,10 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
     /* pageable sources: each copy has taken its bytes when the call returns */
     RSC_CUDA(cudaMemcpyAsync(b->d_adv, b->h_adv.data(), n * sizeof(rsc::BatchAdvance), cudaMemcpyHostToDevice, b->stream));
     RSC_CUDA(cudaMemcpyAsync(b->d_pulse, b->h_pulse.data(), n * sizeof(PulseArgs), cudaMemcpyHostToDevice, b->stream));
-    RSC_CUDA(cudaMemcpyAsync(b->d_adv_prefix, b->h_adv_prefix.data(), (n + 1) * sizeof(unsigned), cudaMemcpyHostToDevice,
-                             b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_rain_prefix, b->h_rain_prefix.data(), (n + 1) * sizeof(unsigned),
+                             cudaMemcpyHostToDevice, b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_deb_prefix, b->h_deb_prefix.data(), (n + 1) * sizeof(unsigned),
+                             cudaMemcpyHostToDevice, b->stream));
     RSC_CUDA(cudaMemcpyAsync(b->d_pulse_prefix, b->h_pulse_prefix.data(), (n + 1) * sizeof(unsigned),
                              cudaMemcpyHostToDevice, b->stream));
     return RSC_OK;
@@ -1620,16 +1631,32 @@ cudaError_t batch_launch_pulse(rsc_batch *b, int k) {
     return cudaGetLastError();
 }
 
-/* Steps 0..K-1: pulse of every instance, then the advance of every instance. */
+/* Steps 0..K-1: pulse of every instance, then the advance of every instance
+ * (background kernel on the batch's stream, debris kernel beside it). */
 cudaError_t batch_enqueue(rsc_batch *b, int steps) {
     const int n = (int)b->w.size();
     for (int k = 0; k < steps; k++) {
         cudaError_t e = batch_launch_pulse(b, k);
         if (e != cudaSuccess) return e;
-        if (b->adv_blocks) {
-            rsc::k_advance_batch<<<b->adv_blocks, rsc::kAdvanceThreads, 0, b->stream>>>(
-                b->d_adv, b->d_steps + (size_t)k * n, b->d_adv_prefix, n);
+        const rsc::BatchStep *st = b->d_steps + (size_t)k * n;
+        if (b->deb_blocks) {
+            e = cudaEventRecord(b->fork_ev, b->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork_ev, 0);
+            if (e != cudaSuccess) return e;
+            rsc::k_advance_batch_debris<<<b->deb_blocks, rsc::kAdvanceThreads, 0, b->side>>>(b->d_adv, st,
+                                                                                            b->d_deb_prefix, n);
             e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaEventRecord(b->side_ev, b->side);
+            if (e != cudaSuccess) return e;
+        }
+        if (b->rain_blocks) {
+            rsc::k_advance_batch_rain<<<b->rain_blocks, rsc::kAdvanceThreads, 0, b->stream>>>(b->d_adv, st,
+                                                                                             b->d_rain_prefix, n);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        if (b->deb_blocks) {
+            e = cudaStreamWaitEvent(b->stream, b->side_ev, 0);
             if (e != cudaSuccess) return e;
         }
     }
@@ -1776,6 +1803,11 @@ int rsc_batch_create(rsc_worker *const *workers, int count, rsc_batch **out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_h2d, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking);
+    int prio_least = 0, prio_greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, prio_greatest);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->side_ev, cudaEventDisableTiming);
     b->slot_used.assign(2 * count, nullptr);
     b->slot_ready.assign(2 * count, nullptr);
     b->slot_pending.assign(2 * count, 0);
@@ -1785,7 +1817,8 @@ int rsc_batch_create(rsc_worker *const *workers, int count, rsc_batch **out) {
     }
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_adv, count * sizeof(rsc::BatchAdvance));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulse, count * sizeof(PulseArgs));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_adv_prefix, (count + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_rain_prefix, (count + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_deb_prefix, (count + 1) * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulse_prefix, (count + 1) * sizeof(unsigned));
     if (e != cudaSuccess) {
         rsc_batch_free(b);
@@ -1805,7 +1838,8 @@ int rsc_batch_free(rsc_batch *b) {
     free_ptr(b->d_out);
     free_ptr(b->d_adv);
     free_ptr(b->d_pulse);
-    free_ptr(b->d_adv_prefix);
+    free_ptr(b->d_rain_prefix);
+    free_ptr(b->d_deb_prefix);
     free_ptr(b->d_pulse_prefix);
     if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
     free_ptr(b->les_stage);
@@ -1816,6 +1850,12 @@ int rsc_batch_free(rsc_batch *b) {
         if (ev) cudaEventDestroy(ev);
     }
     if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
+    if (b->side) {
+        cudaStreamSynchronize(b->side);
+        cudaStreamDestroy(b->side);
+    }
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->side_ev) cudaEventDestroy(b->side_ev);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
     if (b->ev_h2d) cudaEventDestroy(b->ev_h2d);
     if (b->ev_done) cudaEventDestroy(b->ev_done);
@@ -1944,7 +1984,7 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
     } else {
         RSC_CUDA(batch_enqueue(b, steps));
     }
-    b->launches += (uint64_t)steps * (b->adv_blocks ? 2u : 1u);
+    b->launches += (uint64_t)steps * (1u + (b->rain_blocks ? 1u : 0u) + (b->deb_blocks ? 1u : 0u));
     for (size_t q = 0; q < 2 * n; q++) {
         if (used[q]) RSC_CUDA(cudaEventRecord(b->slot_used[q], b->stream));
     }

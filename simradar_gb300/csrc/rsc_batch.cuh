@@ -2,14 +2,15 @@
  * rsc_batch.cuh -- many emulation instances per launch.
  *
  * An instance is one worker: its own scatterer arrays, tables, gates, pulse
- * accumulator and counter.  One time step of every instance is two launches:
- * k_pulse_batch forms every instance's pulse, k_advance_batch advances every
- * instance's scatterers.  Blocks are assigned to instances in proportion to
+ * accumulator and counter.  One time step of every instance is three
+ * launches: k_pulse_batch forms every instance's pulse, k_advance_batch_rain
+ * advances every instance's background range and k_advance_batch_debris,
+ * beside it on a high-priority stream, every instance's debris.  Blocks are assigned to instances in proportion to
  * their work through a prefix table; each block copies its instance's launch
  * descriptor into shared memory, takes the step's beam / time / LES slot from
  * the per-step table, and runs the same block bodies as the one-instance
  * kernels (so every instance's state evolves bit for bit as it would alone).
- * A run of K steps is 2 K launches whose arguments differ only in the step
+ * A run of K steps is 3 K launches whose arguments differ only in the step
  * index, which is what lets the host capture it once in a CUDA graph.
  */
 #ifndef SIMRADAR_GB300_RSC_BATCH_CUH
@@ -56,10 +57,10 @@ __device__ __forceinline__ void block_copy(void *dst, const void *src, unsigned 
     for (unsigned k = threadIdx.x; k < bytes / 4; k += blockDim.x) d[k] = __ldg(s + k);
 }
 
-__global__ void __launch_bounds__(kAdvanceThreads, 4)
-k_advance_batch(const BatchAdvance *inst, const BatchStep *steps, const unsigned *prefix, int ninst) {
-    __shared__ __align__(16) AdvanceArgs sa;
-    __shared__ int s_i;
+/* The instance of this block and its advance descriptor for the step, in
+ * shared memory; returns the instance. */
+__device__ __forceinline__ int batch_advance_args(AdvanceArgs &sa, int &s_i, const BatchAdvance *inst,
+                                                  const BatchStep *steps, const unsigned *prefix, int ninst) {
     if (threadIdx.x == 0) s_i = batch_instance(prefix, ninst, blockIdx.x);
     __syncthreads();
     const int i = s_i;
@@ -73,7 +74,45 @@ k_advance_batch(const BatchAdvance *inst, const BatchStep *steps, const unsigned
         sa.dff = inst[i].dff[les];
     }
     __syncthreads();
-    advance_body(sa, blockIdx.x - __ldg(prefix + i));
+    return i;
+}
+
+/* The background range of every instance (prefix over their background
+ * blocks); the rain body chosen per instance by its concept.  6 resident
+ * blocks per SM measured faster than 5 despite a few spilled registers. */
+__global__ void __launch_bounds__(kAdvanceThreads, 6)
+k_advance_batch_rain(const BatchAdvance *inst, const BatchStep *steps, const unsigned *prefix, int ninst) {
+    __shared__ __align__(16) AdvanceArgs sa;
+    __shared__ int s_i;
+    const int i = batch_advance_args(sa, s_i, inst, steps, prefix, ninst);
+    const unsigned long long j = (unsigned long long)(blockIdx.x - __ldg(prefix + i)) * kAdvanceThreads + threadIdx.x;
+    if (j >= sa.rain_count) return;
+    const size_t x = (size_t)(sa.rain_origin + j);
+    float4 pos, rcs;
+    bool known;
+    if (sa.rain_mode == 1) {
+        rain_el(sa, x, pos, rcs, known);
+    } else if (sa.rain_mode == 0) {
+        rain_bg(sa, x, pos, rcs, known);
+    } else {
+        rain_fp(sa, x, pos, rcs, known);
+    }
+}
+
+/* The debris ranges of every instance (prefix over their debris blocks), run
+ * beside k_advance_batch_rain on a high-priority stream. */
+__global__ void __launch_bounds__(kAdvanceThreads)
+k_advance_batch_debris(const BatchAdvance *inst, const BatchStep *steps, const unsigned *prefix, int ninst) {
+    __shared__ __align__(16) AdvanceArgs sa;
+    __shared__ int s_i;
+    const int i = batch_advance_args(sa, s_i, inst, steps, prefix, ninst);
+    const unsigned long long j = (unsigned long long)(blockIdx.x - __ldg(prefix + i)) * kAdvanceThreads + threadIdx.x;
+    if (sa.ntypes == 0 || j >= sa.deb_prefix[sa.ntypes]) return;
+    const int t = debris_type_of(sa, j);
+    const DebrisType &T = sa.types[t];
+    float4 pos, rcs;
+    bool known;
+    debris_step(sa, T, (size_t)(T.origin + (j - sa.deb_prefix[t])), pos, rcs, known);
 }
 
 template <int MODE>

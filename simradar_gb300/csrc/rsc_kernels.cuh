@@ -296,8 +296,6 @@ __device__ __forceinline__ int debris_type_of(const AdvanceArgs &a, unsigned lon
     return t;
 }
 
-/* block b of one time step: blocks [0, rain_blocks) take the background
- * range, the rest the concatenated debris ranges */
 /* One scatterer of block b of a time step (blocks [0, rain_blocks) take the
  * background, the rest the debris types in order): advanced in memory, and
  * its new position and backscatter returned for a pulse formed in the same
@@ -337,20 +335,13 @@ __device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, un
     return advance_one_t<-1>(a, b, i_out, pos, rcs);
 }
 
-__device__ __forceinline__ void advance_body(const AdvanceArgs &a, unsigned b) {
-    unsigned long long i;
-    float4 pos, rcs;
-    (void)advance_one(a, b, i, pos, rcs);
-}
-
-/* 5 blocks of 256 per SM (<= 51 registers): the step is a chain of dependent
- * loads (state, then 8 LES texels, then the debris tables), so resident warps
- * are what hides the latency */
 /* One time step as two kernels: the background kernel holds only its own
  * (short) path, which the debris path's code slows by about a tenth when both
- * share one kernel; the host runs the debris kernel beside it on a second
- * stream.  The batched and fused kernels take both paths through
- * advance_one. */
+ * share one kernel; the host runs the debris kernel beside it on a second,
+ * high-priority stream.  6 blocks of 256 per SM (<= 42 registers): the step
+ * is a chain of dependent loads (state, then the LES texel pairs), so
+ * resident warps are what hides the latency.  The fused step kernel takes
+ * both paths through advance_one. */
 template <int RAIN_MODE>
 __global__ void __launch_bounds__(kAdvanceThreads, 6) k_advance_rain(const AdvanceArgs a) {
     const unsigned long long j = (unsigned long long)blockIdx.x * kAdvanceThreads + threadIdx.x;

@@ -321,6 +321,7 @@ int acquire(rsc_les_source *s, uint32_t frame, Held *out, const char **why) {
 }
 
 int pin(rsc_les_source *s, const Held &h, const char **why) {
+    std::lock_guard<std::mutex> lock(s->mu);   /* callers holding the same buffer */
     Entry &E = s->e[h.entry];
     if (E.pinned) return RSC_OK;
     cudaError_t e = cudaHostRegister(E.planes, s->nn * kPlanes * sizeof(float), cudaHostRegisterPortable);

@@ -352,7 +352,7 @@ class Worker:
 
 
 class Batch:
-    """Many workers stepped together: two launches per step for all of them
+    """Many workers stepped together: three launches per step for all of them
     (the batching form of include/rsc.h).  Keeps references to the workers so
     they outlive the batch."""
 

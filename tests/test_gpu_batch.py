@@ -1,6 +1,6 @@
-"""GPU parity of the batching form: many instances stepped by two launches per
-step (one pulse launch and one advance launch for all of them), with and
-without a CUDA graph.
+"""GPU parity of the batching form: many instances stepped by three launches
+per step (the pulse, the background advance and the debris advance, each for
+all of them), with and without a CUDA graph.
 
 Every instance must evolve bit for bit as the oracle does for it alone, and
 its pulses must agree with the exact FP32 sum within the same bound as the
@@ -82,7 +82,7 @@ def test_batch_matches_oracle(backend, oracle_lib, scenes):
                 O.advance_time(sts[i], S, S.counts, S.les[les[j, i]], sd)
         for i, W in enumerate(ws):
             assert_state_equal(W.download(STATE_FIELDS), sts[i].s, where="instance %d after step %d " % (i, k0 + 2))
-    assert B.launch_count == 12
+    assert B.launch_count == 18   # per step: pulse, background advance, debris advance
     # respawns happened in the big instance and were reproduced
     assert (bits(sts[0].s["rnd"]) != bits(scenes[0].state["rnd"])).any(axis=1).sum() >= 64
     B.close()

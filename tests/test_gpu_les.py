@@ -104,3 +104,43 @@ def test_upload_beside_set_les(backend, tmp_path):
     A.close()
     B.close()
     src.close()
+
+
+def test_batch_reads_uploaded_slot(backend, oracle_lib, tmp_path):
+    """A batch run that reads a slot filled by rsc_les_upload_async waits for
+    the upload: two instances, one of them switching to the uploaded frame."""
+    S, d = scene_and_folder(tmp_path, "suctvort")
+    src = backend.LESSource(d, "suctvort")
+    S.les_desc = src.descriptor()
+    T = synth.make_scene(num_rain=5000, les_cfg=S.les_cfg, with_tables=False, seed=31)
+    T.les, T.les_desc = S.les, S.les_desc
+    scenes = (S, T)
+    ws = []
+    for X in scenes:
+        W = backend.Worker(0)
+        synth.load_worker(W, X, les_slot_volumes=())
+        src.upload_async(W, 0, 0)
+        ws.append(W)
+    B = backend.Batch(ws)
+    B.set_populations([synth.population(X) for X in scenes])
+    sts = [oracle_lib.OracleState(X.state) for X in scenes]
+    vols = {f: oracle_volume(d, "suctvort", f) for f in (0, 2)}
+    src.upload_async(ws[0], 1, 2)   # instance 0, slot 1 <- frame 2, queued before the run
+    steps = 3
+    sims = np.zeros((steps, 2, 16), np.float32)
+    les = np.zeros((steps, 2), np.int32)
+    for j in range(steps):
+        for i, X in enumerate(scenes):
+            sims[j, i] = synth.pulse_sim_desc(X, j + i, tic=j * 1e-3)
+        les[j, 0] = 1
+    B.run(sims, les, use_graph=True)
+    B.synchronize()
+    for j in range(steps):
+        for i, X in enumerate(scenes):
+            oracle_lib.advance_time(sts[i], X, X.counts, vols[2 if i == 0 else 0], sims[j, i])
+    for i, W in enumerate(ws):
+        assert_state_equal(W.download(STATE_FIELDS), sts[i].s, where="instance %d " % i)
+    B.close()
+    for W in ws:
+        W.close()
+    src.close()
