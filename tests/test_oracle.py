@@ -71,8 +71,12 @@ def test_make_pulse_known_answer(oracle_lib):
     rc = L.or_make_pulse(O.fp(pulse), O.fp(sig), O.fp(aux), O.fp(pos), O.fp(rcs), n, n, O.fp(aw), O.fp(awd),
                          O.fp(rw), O.fp(rwd), float(r0), float(dr), G, O.fp(sd), 64, 64, 49152, 0)
     assert rc == 0
-    # CPU loop of test_make_pulse.c:553-583 (float32, sequential sums)
-    r_a = aux[:, 0]
+    cpu = kat_cpu_pulse(pos, rcs, aux[:, 0], sd, rw, rwd, aw, awd, G, r0, dr)
+    assert_kat(pulse, cpu)
+
+
+def kat_cpu_pulse(pos, rcs, r_a, sd, rw, rwd, aw, awd, G, r0, dr):
+    """The CPU loop of test_make_pulse.c:553-583 (float32, sequential sums)."""
     ang = np.arccos(((sd[0] * pos[:, 0] + sd[1] * pos[:, 1] + sd[2] * pos[:, 2]) / r_a).astype(np.float32))
     w_a = read_table(aw, awd[2], (ang * awd[0] + awd[1]).astype(np.float32))
     atten = np.power(r_a, F(-2.0)).astype(np.float32)
@@ -86,11 +90,15 @@ def test_make_pulse_known_answer(oracle_lib):
         w_r = read_table(rw, rwd[2], ((r_a - r) * rwd[0] + rwd[1]).astype(np.float32))
         contrib = (sig_cpu * (w_r * w_a)[:, None]).astype(np.float32)
         cpu[ir] = np.cumsum(contrib, axis=0, dtype=np.float32)[-1]
-    # the reference's green / red rule (test_make_pulse.c:640-646)
+    return cpu
+
+
+def assert_kat(pulse, cpu):
+    """The reference's green / red rule (test_make_pulse.c:640-646) on gate
+    lane 0, and a tighter check of all four lanes."""
     delta = (cpu[:, 0] - pulse[:, 0]) / np.maximum(1.0, pulse[:, 0])
     square = cpu[:, 0] ** 2 + cpu[:, 1] ** 2
     assert np.all(delta / np.maximum(1.0, square) < 1e-3)
-    # and a tighter check of all four lanes
     assert np.allclose(pulse, cpu, rtol=2e-3, atol=1e-3 * np.abs(cpu).max())
 
 
