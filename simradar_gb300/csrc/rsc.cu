@@ -260,6 +260,14 @@ Image make_image(const float4 *d, uint32_t nx, uint32_t ny, uint32_t nz) {
     return im;
 }
 
+/* The range weight table is RS_set_range_weight_to_triangle's {0, 1, 0}
+ * (entries compared bit for bit: a -0 would change the mix) with origin 1
+ * and max 2, which the pulse kernel evaluates by range_weight_tri. */
+bool is_triangle(uint32_t n, const float *w4, const float *desc) {
+    static const float tri[3] = {0.0f, 1.0f, 0.0f};
+    return n == 3 && memcmp(w4, tri, sizeof(tri)) == 0 && desc[1] == 1.0f && desc[2] == 2.0f;
+}
+
 rsc::PairImage make_pair_image(const float4 *d, uint32_t nx, uint32_t ny, uint32_t nz) {
     rsc::PairImage im;
     im.data = d;
@@ -471,6 +479,7 @@ void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
     P.rdelta = w->range_delta;
     P.rw_n = w->range_n;
     memcpy(P.rwv, w->range_weight_small, sizeof(P.rwv));
+    P.rw_tri = is_triangle(w->range_n, w->range_weight_small, w->range_desc) ? 1 : 0;
     P.acc64 = w->acc64;
     P.counter = w->counter;
     P.coherent_span = w->perm != nullptr ? (int)w->G + 1 : 0;
@@ -2194,6 +2203,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     P.rdelta = range_delta;
     P.rw_n = range_n;
     for (uint32_t k = 0; k < 4; k++) P.rwv[k] = k < range_n ? range_weight[k] : 0.0f;
+    P.rw_tri = is_triangle(range_n, P.rwv, range_desc) ? 1 : 0;
     P.acc64 = reinterpret_cast<double *>(b + RSC_NA_ACC_OFF);
     P.counter = reinterpret_cast<unsigned *>(b + RSC_NA_COUNTER_OFF);
     P.pulse = reinterpret_cast<float4 *>(pulse4);

@@ -397,6 +397,7 @@ struct PulseArgs {
     float rdelta;        /* gate spacing: the running sum's increment */
     unsigned rw_n;       /* range weight table length; <= 4 is kept in rwv */
     float rwv[4];
+    int rw_tri;          /* the table is the triangle {0, 1, 0} with origin 1 and max 2 */
     int dense;
     int coherent_span;   /* warp-coherent gate path when a warp spans fewer gates */
     int materialize;
@@ -416,9 +417,27 @@ __device__ __forceinline__ float range_weight(const PulseArgs &P, float d) {
     return cl_mix(__ldg(P.rw + (uint32_t)f0), __ldg(P.rw + (uint32_t)f1), dec0);
 }
 
+/* The weight of the triangle table {0, 1, 0} with origin 1 and max 2 (what
+ * RS_set_range_weight_to_triangle sets, rs.c:2620-2623), bit for bit the
+ * value range_weight's two clamped indices, table picks and mix give on it:
+ * on the rising side (index x0 in [0, 1)) the mix is 0 + (1 - 0) x0 = x0,
+ * unless the second index has already rounded up to the last entry (x1 = 2,
+ * a rounding corner within 2^-24 of the peak), where both picks are 0; on
+ * the falling side (x0 in [1, 2)) it is 1 + (0 - 1)(x0 - 1), one rounding of
+ * 1 - (x0 - 1); at x0 = 2 it is 0.  Checked against range_weight on 1.8e8
+ * arguments around every breakpoint. */
+__device__ __forceinline__ float range_weight_tri(const PulseArgs &P, float d) {
+    const float x0 = cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, 2.0f);
+    const float x1 = cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 1.0f), 0.0f, 2.0f);
+    const float up = x1 < 2.0f ? x0 : 0.0f;
+    const float down = x0 < 2.0f ? 1.0f - (x0 - 1.0f) : 0.0f;
+    return x0 < 1.0f ? up : down;
+}
+
 /* the same weight with a table of at most 4 entries held in the kernel
  * parameters (the triangle of RS_set_range_weight_to_triangle has 3) */
 __device__ __forceinline__ float range_weight_reg(const PulseArgs &P, float d) {
+    if (P.rw_tri) return range_weight_tri(P, d);
     if (P.rw_n > 4) return range_weight(P, d);
     float f0, f1;
     float dec0 = cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, P.rwd[2]), &f0);

@@ -53,6 +53,24 @@ __device__ __forceinline__ float weight_comp(const float *W, const float *desc, 
     return fmaf(w1 - w0, frac, w0);
 }
 
+/* The compensated range weight.  On the triangle {0, 1, 0} with origin 1 and
+ * max 2 the weight is 1 - |t| for t = index - 1 = p + pe, with p + pe the
+ * double-float (a_hi + a_lo) s: no addition of the origin.  With sg the
+ * sign of t, 1 - |t| = (1 - sg p) - sg pe, where 1 - sg p is exact for the
+ * |p| within a factor 2 of 1 where the weight is small, and the tail joins
+ * in one rounding: the weight keeps its relative accuracy up to the edges of
+ * the support (1.2e-7 against 3e-5 for weight_comp, whose 1 - frac cancels
+ * there).  Other tables go through weight_comp. */
+__device__ __forceinline__ float range_weight_comp(const float *W, const float *desc, int tri, float a_hi,
+                                                   float a_lo) {
+    if (!tri) return weight_comp(W, desc, a_hi, a_lo);
+    const float s = desc[0];
+    const float p = a_hi * s;
+    const float pe = fmaf(a_hi, s, -p) + a_lo * s;
+    const float sg = (p + pe) < 0.0f ? -1.0f : 1.0f;
+    return fmaxf((1.0f - sg * p) - sg * pe, 0.0f);
+}
+
 /* double-float helpers: (hi, lo) with |lo| <= ulp(hi) / 2 */
 __device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float &h, float &l) {
     float s, e;
@@ -362,7 +380,8 @@ struct PulseBins {
                     float w = 0.0f;
                     if (gate >= k_lo && gate <= k_hi) {
                         if constexpr (MODE == 1) {
-                            w = weight_comp(P.rw, P.rwd, r - __ldg(P.rk + gate), r_lo - __ldg(P.rk_lo + gate));
+                            w = range_weight_comp(P.rw, P.rwd, P.rw_tri, r - __ldg(P.rk + gate),
+                                                  r_lo - __ldg(P.rk_lo + gate));
                         } else {
                             w = range_weight_reg(P, r - rkj);
                         }
@@ -387,7 +406,8 @@ struct PulseBins {
                     if (gate <= k_hi) {
                         float w;
                         if constexpr (MODE == 1) {
-                            w = weight_comp(P.rw, P.rwd, r - __ldg(P.rk + gate), r_lo - __ldg(P.rk_lo + gate));
+                            w = range_weight_comp(P.rw, P.rwd, P.rw_tri, r - __ldg(P.rk + gate),
+                                                  r_lo - __ldg(P.rk_lo + gate));
                         } else {
                             w = range_weight_reg(P, r - rkj);
                         }
