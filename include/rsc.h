@@ -439,7 +439,9 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
 
 /* Diagnostics: evaluate the shared elementary functions (rsmath.h) on the
  * device; fn: 0 sin, 1 cos, 2 log, 3 log1p, 4 acos, 5 atan2(a, b), 6 exp,
- * 7 pow(a, b).  Host arrays of n floats. */
+ * 7 pow(a, b), 8 the pulse kernel's closed-form range weight of distance a
+ * on the triangle table {0, 1, 0} with scale b, origin 1, max 2.  Host
+ * arrays of n floats. */
 int rsc_eval_math(int fn, const float *a, const float *b, float *out, size_t n);
 
 #ifdef __cplusplus

@@ -947,6 +947,16 @@ void or_eval_math(int fn, const float *a, const float *b, float *out, size_t n) 
             case 5: out[i] = rsm_atan2f(a[i], b[i]); break;
             case 6: out[i] = rsm_expf(a[i]); break;
             case 7: out[i] = rsm_powf(a[i], b[i]); break;
+            case 8: {
+                /* the pass-1 range weight (rs.cl:1196-1209) of d = a[i] on the
+                 * triangle {0, 1, 0} with scale b[i], origin 1, max 2 */
+                static const float W[3] = {0.0f, 1.0f, 0.0f};
+                float f0, f1;
+                const float dec0 = cl_fract(cl_clamp(fmaf(a[i], b[i], 1.0f + 0.0f), 0.0f, 2.0f), &f0);
+                (void)cl_fract(cl_clamp(fmaf(a[i], b[i], 1.0f + 1.0f), 0.0f, 2.0f), &f1);
+                out[i] = cl_mix(W[(uint32_t)f0], W[(uint32_t)f1], dec0);
+                break;
+            }
             default: out[i] = 0.0f; break;
         }
     }

@@ -424,11 +424,11 @@ __device__ __forceinline__ float range_weight(const PulseArgs &P, float d) {
  * unless the second index has already rounded up to the last entry (x1 = 2,
  * a rounding corner within 2^-24 of the peak), where both picks are 0; on
  * the falling side (x0 in [1, 2)) it is 1 + (0 - 1)(x0 - 1), one rounding of
- * 1 - (x0 - 1); at x0 = 2 it is 0.  Checked against range_weight on 1.8e8
- * arguments around every breakpoint. */
-__device__ __forceinline__ float range_weight_tri(const PulseArgs &P, float d) {
-    const float x0 = cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, 2.0f);
-    const float x1 = cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 1.0f), 0.0f, 2.0f);
+ * 1 - (x0 - 1); at x0 = 2 it is 0.  The GPU test of rsc_eval_math function
+ * 8 compares it with the oracle's table lerp around every breakpoint. */
+__device__ __forceinline__ float range_weight_tri(const float *rwd, float d) {
+    const float x0 = cl_clamp(fmaf(d, rwd[0], rwd[1] + 0.0f), 0.0f, 2.0f);
+    const float x1 = cl_clamp(fmaf(d, rwd[0], rwd[1] + 1.0f), 0.0f, 2.0f);
     const float up = x1 < 2.0f ? x0 : 0.0f;
     const float down = x0 < 2.0f ? 1.0f - (x0 - 1.0f) : 0.0f;
     return x0 < 1.0f ? up : down;
@@ -437,7 +437,7 @@ __device__ __forceinline__ float range_weight_tri(const PulseArgs &P, float d) {
 /* the same weight with a table of at most 4 entries held in the kernel
  * parameters (the triangle of RS_set_range_weight_to_triangle has 3) */
 __device__ __forceinline__ float range_weight_reg(const PulseArgs &P, float d) {
-    if (P.rw_tri) return range_weight_tri(P, d);
+    if (P.rw_tri) return range_weight_tri(P.rwd, d);
     if (P.rw_n > 4) return range_weight(P, d);
     float f0, f1;
     float dec0 = cl_fract(cl_clamp(fmaf(d, P.rwd[0], P.rwd[1] + 0.0f), 0.0f, P.rwd[2]), &f0);
@@ -692,6 +692,11 @@ __global__ void k_eval_math(int fn, const float *a, const float *b, float *out, 
         case 5: out[i] = rsm_atan2f(a[i], b[i]); break;
         case 6: out[i] = rsm_expf(a[i]); break;
         case 7: out[i] = rsm_powf(a[i], b[i]); break;
+        case 8: {   /* the triangle range weight of d = a[i], scale b[i] */
+            const float rwd[4] = {b[i], 1.0f, 2.0f, 0.0f};
+            out[i] = range_weight_tri(rwd, a[i]);
+            break;
+        }
         default: out[i] = 0.0f; break;
     }
 }

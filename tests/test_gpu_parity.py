@@ -100,6 +100,40 @@ def test_math_bitexact(backend, oracle_lib):
         assert np.array_equal(bits(g), bits(c)), "math fn %d differs on %d inputs" % (fn, int((bits(g) != bits(c)).sum()))
 
 
+def _ulp_walk(x, k):
+    """x moved k representable floats (k < 0: down)."""
+    x = np.float32(x)
+    for _ in range(abs(int(k))):
+        x = np.nextafter(x, np.float32(-np.inf if k < 0 else np.inf), dtype=np.float32)
+    return x
+
+
+def test_triangle_weight_matches_table_lerp(backend, oracle_lib):
+    """The pulse kernel's closed-form weight on the reference's triangle
+    table against the table lerp of make_pulse_pass_1 (rs.cl:1196-1209):
+    bit-identical on random distances and on every float within 40 ulps of
+    the breakpoints -dr, 0 and +dr (the corners of its two index
+    computations), for several gate widths."""
+    rng = np.random.default_rng(11)
+    d_all, s_all = [], []
+    for dr in (30.0, 25.0, 15.0, 7.5, 1.0, 0.3, 150.0, 3.0e-3):
+        s = np.float32(np.float32(1.0) / np.float32(dr))
+        d = list(rng.uniform(-2.5 * dr, 2.5 * dr, 200000).astype(np.float32))
+        for c in (-dr, dr):
+            d += [_ulp_walk(c, k) for k in range(-40, 41)]
+        d += list((np.float32(dr) * np.float32(2.0) ** -np.arange(1, 60, dtype=np.float32)).astype(np.float32))
+        d += list(-(np.float32(dr) * np.float32(2.0) ** -np.arange(1, 60, dtype=np.float32)).astype(np.float32))
+        d += [np.float32(0.0), np.float32(-0.0), np.float32(np.nan), np.float32(np.inf), np.float32(-np.inf)]
+        d_all += d
+        s_all += [s] * len(d)
+    a = np.array(d_all, np.float32)
+    b = np.array(s_all, np.float32)
+    g = backend.eval_math(8, a, b)
+    c = oracle_lib.eval_math(8, a, b)
+    assert np.array_equal(bits(g), bits(c)), "triangle weight differs on %d of %d inputs" % (
+        int((bits(g) != bits(c)).sum()), a.size)
+
+
 def test_advance_dbu_bitexact(backend, oracle_lib, scene_db):
     """Concept DBU (el_atts, bounded) rain + three debris types, 6 steps."""
     W, st, _ = run_pair(backend, oracle_lib, scene_db, 6)
