@@ -372,12 +372,19 @@ typedef void (*PulseKernel)(const PulseArgs);
  * the path at run time (one compensated kernel per path measured 7% slower). */
 PulseKernel pulse_kernel(int mode, int path) {
     if (mode == RSC_PULSE_PLAIN) {
+        if (path == 3) return rsc::k_pulse_pairs;
         return path == 2 ? rsc::k_pulse<0, 2> : (path == 1 ? rsc::k_pulse<0, 1> : rsc::k_pulse<0, 0>);
     }
     return mode == RSC_PULSE_COMPENSATED ? rsc::k_pulse<1, -1> : rsc::k_pulse<2, -1>;
 }
 
-int pulse_path(const PulseArgs &P) { return P.dense ? 2 : (P.coherent_span > 0 ? 1 : 0); }
+/* 0 atomics, 1 coherent warps, 2 every gate, 3 coherent warps with two
+ * scatterers per lane (the plain form when it does not write aux / sig) */
+int pulse_path(const PulseArgs &P, int mode) {
+    if (P.dense) return 2;
+    if (P.coherent_span <= 0) return 0;
+    return (mode == RSC_PULSE_PLAIN && !P.materialize) ? 3 : 1;
+}
 
 /* Launch shape of the pulse kernel (one-instance or batched form) for G
  * gates: warps per block as many as fit 200 KB of bins (at most 16, at most
@@ -455,7 +462,7 @@ cudaError_t launch_advance(rsc_worker *w, const AdvanceArgs &a, unsigned blocks,
 }
 
 void launch_pulse(int mode, const PulseArgs &P, int grid, int threads, size_t smem, cudaStream_t st) {
-    pulse_kernel(mode, pulse_path(P))<<<grid, threads, smem, st>>>(P);
+    pulse_kernel(mode, pulse_path(P, mode))<<<grid, threads, smem, st>>>(P);
 }
 
 void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
@@ -1324,14 +1331,14 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     if (mode == RSC_PULSE_COMPENSATED) {
         P.rk = w->rk_hi;
     }
+    const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
+    P.materialize = mat ? 1 : 0;
     int grid = 0, threads = 0;
     size_t smem = 0;
-    s = pulse_geometry(w, mode, pulse_path(P), &grid, &threads, &smem);
+    s = pulse_geometry(w, mode, pulse_path(P, mode), &grid, &threads, &smem);
     if (s) return s;
     s = pulse_d2h_wait(w);
     if (s) return s;
-    const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
-    P.materialize = mat ? 1 : 0;
     if (w->pend && mode != RSC_PULSE_F64) {
         /* the recorded advance and this pulse in one pass over the state */
         int sgrid = 0;
@@ -1758,7 +1765,7 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
         for (int per_sm = 1; per_sm <= 4; per_sm++) {
             int got = 0, threads = 0;
             size_t smem = 0;
-            s = pulse_shape(mode, false, w->G, warps, per_sm, &got, &threads, &smem, pulse_path(P));
+            s = pulse_shape(mode, false, w->G, warps, per_sm, &got, &threads, &smem, pulse_path(P, mode));
             if (s) return s;
             if (threads != warps * 32 || got != per_sm) continue;   /* shape not reachable */
             const int grid = w->num_sms * per_sm;
@@ -2225,7 +2232,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
         }
     }
     /* launch geometry of the plain pulse kernel, capped to the scratch size */
-    const PulseKernel kern = pulse_kernel(RSC_PULSE_PLAIN, pulse_path(P));
+    const PulseKernel kern = pulse_kernel(RSC_PULSE_PLAIN, pulse_path(P, RSC_PULSE_PLAIN));
     int dev = 0, sms = 0, per_sm = 1;
     RSC_CUDA(cudaGetDevice(&dev));
     RSC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

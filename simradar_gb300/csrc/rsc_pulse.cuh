@@ -485,6 +485,63 @@ struct PulseBins {
         }
     }
 
+    /* Two scatterers per lane (plain form, state in spatial order): lane l
+     * holds scatterers a and b of a run of 64 neighbours, the warp visits
+     * the gates of both together and each lane adds its two weighted
+     * signals before the one warp reduction per gate (half the reductions
+     * of two add calls).  The weights are those of add, bit for bit (the
+     * same running-sum gate origin from the warp's first gate).  A warp with
+     * a non-finite signal takes its scatterers one at a time through add. */
+    __device__ __forceinline__ void add2(const PulseArgs &P, bool in_a, unsigned long long ia, float4 pa, float4 xa,
+                                         bool in_b, unsigned long long ib, float4 pb, float4 xb) {
+        static_assert(MODE == 0, "the paired form is the plain one");
+        Sig32 sa, sb;
+        sa.r = sb.r = 0.0f;
+        sa.s.set(0.0f, 0.0f, 0.0f, 0.0f);
+        sb.s.set(0.0f, 0.0f, 0.0f, 0.0f);
+        bool fa = false, fb = false;
+        if (in_a) {
+            signal_plain(P, pa, xa, sa);
+            fa = fabsf(sa.r) < INFINITY && finite4(sa.s.v);
+        }
+        if (in_b) {
+            signal_plain(P, pb, xb, sb);
+            fb = fabsf(sb.r) < INFINITY && finite4(sb.s.v);
+        }
+        if (__any_sync(0xffffffffu, (in_a && !fa) || (in_b && !fb))) {
+            add(P, in_a, ia, pa, xa);
+            add(P, in_b, ib, pb, xb);
+            return;
+        }
+        int alo = 0, ahi = -1, blo = 0, bhi = -1;
+        if (in_a) {
+            const float g = (sa.r - P.rs) * P.inv_delta;
+            alo = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
+            ahi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
+        }
+        if (in_b) {
+            const float g = (sb.r - P.rs) * P.inv_delta;
+            blo = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
+            bhi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
+        }
+        const bool ha = ahi >= alo, hb = bhi >= blo;
+        const unsigned lo = min(ha ? (unsigned)alo : 0xffffffffu, hb ? (unsigned)blo : 0xffffffffu);
+        const unsigned hi = max(ha ? (unsigned)ahi : 0u, hb ? (unsigned)bhi : 0u);
+        const int w_lo = (int)__reduce_min_sync(0xffffffffu, lo);
+        const int w_hi = (int)__reduce_max_sync(0xffffffffu, (ha || hb) ? hi : 0u);
+        if (w_lo == -1) return;   /* no lane reaches a gate */
+        float rkj = __ldg(P.rk + w_lo);
+        for (int gate = w_lo; gate <= w_hi; gate++) {
+            float wa = 0.0f, wb = 0.0f;
+            if (gate >= alo && gate <= ahi) wa = range_weight_reg(P, sa.r - rkj);
+            if (gate >= blo && gate <= bhi) wb = range_weight_reg(P, sb.r - rkj);
+            warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, wa * sa.s.v[0] + wb * sb.s.v[0],
+                             wa * sa.s.v[1] + wb * sb.s.v[1], wa * sa.s.v[2] + wb * sb.s.v[2],
+                             wa * sa.s.v[3] + wb * sb.s.v[3]);
+            rkj = rkj + P.rdelta;
+        }
+    }
+
     __device__ __forceinline__ void finish(const PulseArgs &P, unsigned nblk) {
         __syncthreads();
         /* block sum of each output (warp bins in warp order), added into the
@@ -560,6 +617,31 @@ __device__ __forceinline__ void pulse_body(const PulseArgs &P, unsigned blk, uns
 template <int MODE, int PATH>
 __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     pulse_body<MODE, PATH>(P, blockIdx.x, gridDim.x);
+}
+
+/* The plain pulse over a state in spatial order, two scatterers per lane
+ * (PulseBins::add2): warp w of block blk takes runs of 64 neighbours. */
+__global__ void __launch_bounds__(512) k_pulse_pairs(const PulseArgs P) {
+    PulseBins<0, 1> B;
+    B.init(P);
+    const unsigned long long stride = 2ull * gridDim.x * blockDim.x;
+    const unsigned long long n = P.n;
+    const unsigned long long base0 = 2ull * ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    for (unsigned long long base = base0; base < n; base += stride) {
+        const unsigned long long ia = base + B.lane, ib = ia + 32;
+        const bool in_a = ia < n, in_b = ib < n;
+        float4 pa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), xa = pa, pb = pa, xb = pa;
+        if (in_a) {
+            pa = __ldg(P.pos + ia);
+            xa = __ldg(P.rcs + ia);
+        }
+        if (in_b) {
+            pb = __ldg(P.pos + ib);
+            xb = __ldg(P.rcs + ib);
+        }
+        B.add2(P, in_a, ia, pa, xa, in_b, ib, pb, xb);
+    }
+    B.finish(P, gridDim.x);
 }
 
 }  // namespace rsc
