@@ -364,6 +364,11 @@ cudaError_t kernel_occupancy(K kern, int threads, size_t smem, int *per_sm) {
     return e;
 }
 
+/* Scatterers per lane of the grouped plain pulse kernel: 2 measured fastest
+ * (51.7 us against 54.7 for 3 and 62.0 for 4 at README scale: more
+ * registers per lane, fewer resident warps). */
+constexpr int kPulseGroup = 2;
+
 typedef void (*PulseKernel)(const PulseArgs);
 
 /* The one-instance pulse kernel for a mode and a gate path (0 atomics, 1
@@ -372,14 +377,15 @@ typedef void (*PulseKernel)(const PulseArgs);
  * the path at run time (one compensated kernel per path measured 7% slower). */
 PulseKernel pulse_kernel(int mode, int path) {
     if (mode == RSC_PULSE_PLAIN) {
-        if (path == 3) return rsc::k_pulse_pairs;
+        if (path == 3) return rsc::k_pulse_group<kPulseGroup>;
         return path == 2 ? rsc::k_pulse<0, 2> : (path == 1 ? rsc::k_pulse<0, 1> : rsc::k_pulse<0, 0>);
     }
     return mode == RSC_PULSE_COMPENSATED ? rsc::k_pulse<1, -1> : rsc::k_pulse<2, -1>;
 }
 
-/* 0 atomics, 1 coherent warps, 2 every gate, 3 coherent warps with two
- * scatterers per lane (the plain form when it does not write aux / sig) */
+/* 0 atomics, 1 coherent warps, 2 every gate, 3 coherent warps with
+ * kPulseGroup scatterers per lane (the plain form when it does not write
+ * aux / sig) */
 int pulse_path(const PulseArgs &P, int mode) {
     if (P.dense) return 2;
     if (P.coherent_span <= 0) return 0;

@@ -485,59 +485,67 @@ struct PulseBins {
         }
     }
 
-    /* Two scatterers per lane (plain form, state in spatial order): lane l
-     * holds scatterers a and b of a run of 64 neighbours, the warp visits
-     * the gates of both together and each lane adds its two weighted
-     * signals before the one warp reduction per gate (half the reductions
-     * of two add calls).  The weights are those of add, bit for bit (the
-     * same running-sum gate origin from the warp's first gate).  A warp with
-     * a non-finite signal takes its scatterers one at a time through add. */
-    __device__ __forceinline__ void add2(const PulseArgs &P, bool in_a, unsigned long long ia, float4 pa, float4 xa,
-                                         bool in_b, unsigned long long ib, float4 pb, float4 xb) {
-        static_assert(MODE == 0, "the paired form is the plain one");
-        Sig32 sa, sb;
-        sa.r = sb.r = 0.0f;
-        sa.s.set(0.0f, 0.0f, 0.0f, 0.0f);
-        sb.s.set(0.0f, 0.0f, 0.0f, 0.0f);
-        bool fa = false, fb = false;
-        if (in_a) {
-            signal_plain(P, pa, xa, sa);
-            fa = fabsf(sa.r) < INFINITY && finite4(sa.s.v);
+    /* K scatterers per lane (plain form, state in spatial order): lane l
+     * holds scatterers l, l + 32, ... of a run of 32 K neighbours, the warp
+     * visits the gates of all of them together and each lane adds its K
+     * weighted signals before the one warp reduction per gate (1 / K of the
+     * reductions of K add calls).  The weights are those of add, bit for bit
+     * (the same running-sum gate origin from the warp's first gate).  A warp
+     * with a non-finite signal takes its scatterers one at a time through
+     * add. */
+    template <int K>
+    __device__ __forceinline__ void add_k(const PulseArgs &P, const bool *in, const unsigned long long *idx,
+                                          const float4 *pp, const float4 *xx) {
+        static_assert(MODE == 0, "the grouped form is the plain one");
+        float c[K][4], rr[K];
+        int klo[K], khi[K];
+        bool bad = false;
+        unsigned lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            Sig32 sg;
+            sg.r = 0.0f;
+            sg.s.set(0.0f, 0.0f, 0.0f, 0.0f);
+            klo[q] = 0;
+            khi[q] = -1;
+            if (in[q]) {
+                signal_plain(P, pp[q], xx[q], sg);
+                const bool fin = fabsf(sg.r) < INFINITY && finite4(sg.s.v);
+                bad = bad || !fin;
+                const float g = (sg.r - P.rs) * P.inv_delta;
+                klo[q] = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
+                khi[q] = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
+                if (khi[q] >= klo[q]) {
+                    lo = min(lo, (unsigned)klo[q]);
+                    hi = max(hi, (unsigned)khi[q]);
+                }
+            }
+            rr[q] = sg.r;
+            c[q][0] = sg.s.v[0];
+            c[q][1] = sg.s.v[1];
+            c[q][2] = sg.s.v[2];
+            c[q][3] = sg.s.v[3];
         }
-        if (in_b) {
-            signal_plain(P, pb, xb, sb);
-            fb = fabsf(sb.r) < INFINITY && finite4(sb.s.v);
-        }
-        if (__any_sync(0xffffffffu, (in_a && !fa) || (in_b && !fb))) {
-            add(P, in_a, ia, pa, xa);
-            add(P, in_b, ib, pb, xb);
+        if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+            for (int q = 0; q < K; q++) add(P, in[q], idx[q], pp[q], xx[q]);
             return;
         }
-        int alo = 0, ahi = -1, blo = 0, bhi = -1;
-        if (in_a) {
-            const float g = (sa.r - P.rs) * P.inv_delta;
-            alo = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
-            ahi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
-        }
-        if (in_b) {
-            const float g = (sb.r - P.rs) * P.inv_delta;
-            blo = max(0, (int)ceilf(fminf(fmaxf(g - P.win_hi, -1.0f), (float)G)));
-            bhi = min((int)G - 1, (int)floorf(fminf(g - P.win_lo, (float)G)));
-        }
-        const bool ha = ahi >= alo, hb = bhi >= blo;
-        const unsigned lo = min(ha ? (unsigned)alo : 0xffffffffu, hb ? (unsigned)blo : 0xffffffffu);
-        const unsigned hi = max(ha ? (unsigned)ahi : 0u, hb ? (unsigned)bhi : 0u);
         const int w_lo = (int)__reduce_min_sync(0xffffffffu, lo);
-        const int w_hi = (int)__reduce_max_sync(0xffffffffu, (ha || hb) ? hi : 0u);
+        const int w_hi = (int)__reduce_max_sync(0xffffffffu, hi);
         if (w_lo == -1) return;   /* no lane reaches a gate */
         float rkj = __ldg(P.rk + w_lo);
         for (int gate = w_lo; gate <= w_hi; gate++) {
-            float wa = 0.0f, wb = 0.0f;
-            if (gate >= alo && gate <= ahi) wa = range_weight_reg(P, sa.r - rkj);
-            if (gate >= blo && gate <= bhi) wb = range_weight_reg(P, sb.r - rkj);
-            warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, wa * sa.s.v[0] + wb * sb.s.v[0],
-                             wa * sa.s.v[1] + wb * sb.s.v[1], wa * sa.s.v[2] + wb * sb.s.v[2],
-                             wa * sa.s.v[3] + wb * sb.s.v[3]);
+            float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f, v3 = 0.0f;
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const float w = (gate >= klo[q] && gate <= khi[q]) ? range_weight_reg(P, rr[q] - rkj) : 0.0f;
+                v0 = v0 + w * c[q][0];
+                v1 = v1 + w * c[q][1];
+                v2 = v2 + w * c[q][2];
+                v3 = v3 + w * c[q][3];
+            }
+            warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, v0, v1, v2, v3);
             rkj = rkj + P.rdelta;
         }
     }
@@ -619,27 +627,32 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     pulse_body<MODE, PATH>(P, blockIdx.x, gridDim.x);
 }
 
-/* The plain pulse over a state in spatial order, two scatterers per lane
- * (PulseBins::add2): warp w of block blk takes runs of 64 neighbours. */
-__global__ void __launch_bounds__(512) k_pulse_pairs(const PulseArgs P) {
+/* The plain pulse over a state in spatial order, K scatterers per lane
+ * (PulseBins::add_k): warp w of block blk takes runs of 32 K neighbours. */
+template <int K>
+__global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
     PulseBins<0, 1> B;
     B.init(P);
-    const unsigned long long stride = 2ull * gridDim.x * blockDim.x;
+    const unsigned long long stride = (unsigned long long)K * gridDim.x * blockDim.x;
     const unsigned long long n = P.n;
-    const unsigned long long base0 = 2ull * ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    const unsigned long long base0 =
+        (unsigned long long)K * ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
     for (unsigned long long base = base0; base < n; base += stride) {
-        const unsigned long long ia = base + B.lane, ib = ia + 32;
-        const bool in_a = ia < n, in_b = ib < n;
-        float4 pa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), xa = pa, pb = pa, xb = pa;
-        if (in_a) {
-            pa = __ldg(P.pos + ia);
-            xa = __ldg(P.rcs + ia);
+        bool in[K];
+        unsigned long long idx[K];
+        float4 pp[K], xx[K];
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            idx[q] = base + 32u * q + B.lane;
+            in[q] = idx[q] < n;
+            pp[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            xx[q] = pp[q];
+            if (in[q]) {
+                pp[q] = __ldg(P.pos + idx[q]);
+                xx[q] = __ldg(P.rcs + idx[q]);
+            }
         }
-        if (in_b) {
-            pb = __ldg(P.pos + ib);
-            xb = __ldg(P.rcs + ib);
-        }
-        B.add2(P, in_a, ia, pa, xa, in_b, ib, pb, xb);
+        B.template add_k<K>(P, in, idx, pp, xx);
     }
     B.finish(P, gridDim.x);
 }
