@@ -377,19 +377,20 @@ typedef void (*PulseKernel)(const PulseArgs);
  * the path at run time (one compensated kernel per path measured 7% slower). */
 PulseKernel pulse_kernel(int mode, int path) {
     if (mode == RSC_PULSE_PLAIN) {
-        if (path == 3) return rsc::k_pulse_group<kPulseGroup>;
+        if (path == 3) return rsc::k_pulse_group<0, kPulseGroup>;
         return path == 2 ? rsc::k_pulse<0, 2> : (path == 1 ? rsc::k_pulse<0, 1> : rsc::k_pulse<0, 0>);
     }
-    return mode == RSC_PULSE_COMPENSATED ? rsc::k_pulse<1, -1> : rsc::k_pulse<2, -1>;
+    if (mode == RSC_PULSE_COMPENSATED) return path == 3 ? rsc::k_pulse_group<1, kPulseGroup> : rsc::k_pulse<1, -1>;
+    return rsc::k_pulse<2, -1>;
 }
 
 /* 0 atomics, 1 coherent warps, 2 every gate, 3 coherent warps with
- * kPulseGroup scatterers per lane (the plain form when it does not write
- * aux / sig) */
+ * kPulseGroup scatterers per lane (the compensated form, and the plain form
+ * when it does not write aux / sig) */
 int pulse_path(const PulseArgs &P, int mode) {
     if (P.dense) return 2;
     if (P.coherent_span <= 0) return 0;
-    return (mode == RSC_PULSE_PLAIN && !P.materialize) ? 3 : 1;
+    return ((mode == RSC_PULSE_PLAIN && !P.materialize) || mode == RSC_PULSE_COMPENSATED) ? 3 : 1;
 }
 
 /* Launch shape of the pulse kernel (one-instance or batched form) for G

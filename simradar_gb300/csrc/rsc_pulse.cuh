@@ -485,7 +485,8 @@ struct PulseBins {
         }
     }
 
-    /* K scatterers per lane (plain form, state in spatial order): lane l
+    /* K scatterers per lane (plain or compensated form, state in spatial
+     * order): lane l
      * holds scatterers l, l + 32, ... of a run of 32 K neighbours, the warp
      * visits the gates of all of them together and each lane adds its K
      * weighted signals before the one warp reduction per gate (1 / K of the
@@ -496,8 +497,8 @@ struct PulseBins {
     template <int K>
     __device__ __forceinline__ void add_k(const PulseArgs &P, const bool *in, const unsigned long long *idx,
                                           const float4 *pp, const float4 *xx) {
-        static_assert(MODE == 0, "the grouped form is the plain one");
-        float c[K][4], rr[K];
+        static_assert(MODE == 0 || MODE == 1, "the grouped form is the plain or compensated one");
+        float c[K][4], rr[K], rl[K];
         int klo[K], khi[K];
         bool bad = false;
         unsigned lo = 0xffffffffu, hi = 0u;
@@ -505,11 +506,16 @@ struct PulseBins {
         for (int q = 0; q < K; q++) {
             Sig32 sg;
             sg.r = 0.0f;
+            sg.r_lo = 0.0f;
             sg.s.set(0.0f, 0.0f, 0.0f, 0.0f);
             klo[q] = 0;
             khi[q] = -1;
             if (in[q]) {
-                signal_plain(P, pp[q], xx[q], sg);
+                if constexpr (MODE == 0) {
+                    signal_plain(P, pp[q], xx[q], sg);
+                } else {
+                    signal_comp(P, pp[q], xx[q], sg);
+                }
                 const bool fin = fabsf(sg.r) < INFINITY && finite4(sg.s.v);
                 bad = bad || !fin;
                 const float g = (sg.r - P.rs) * P.inv_delta;
@@ -521,6 +527,7 @@ struct PulseBins {
                 }
             }
             rr[q] = sg.r;
+            rl[q] = sg.r_lo;
             c[q][0] = sg.s.v[0];
             c[q][1] = sg.s.v[1];
             c[q][2] = sg.s.v[2];
@@ -534,18 +541,34 @@ struct PulseBins {
         const int w_lo = (int)__reduce_min_sync(0xffffffffu, lo);
         const int w_hi = (int)__reduce_max_sync(0xffffffffu, hi);
         if (w_lo == -1) return;   /* no lane reaches a gate */
-        float rkj = __ldg(P.rk + w_lo);
+        float rkj = MODE == 0 ? __ldg(P.rk + w_lo) : 0.0f;
         for (int gate = w_lo; gate <= w_hi; gate++) {
+            float rk_hi = 0.0f, rk_lo = 0.0f;
+            if constexpr (MODE == 1) {
+                rk_hi = __ldg(P.rk + gate);
+                rk_lo = __ldg(P.rk_lo + gate);
+            }
             float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f, v3 = 0.0f;
 #pragma unroll
             for (int q = 0; q < K; q++) {
-                const float w = (gate >= klo[q] && gate <= khi[q]) ? range_weight_reg(P, rr[q] - rkj) : 0.0f;
+                float w = 0.0f;
+                if (gate >= klo[q] && gate <= khi[q]) {
+                    if constexpr (MODE == 1) {
+                        w = range_weight_comp(P.rw, P.rwd, P.rw_tri, rr[q] - rk_hi, rl[q] - rk_lo);
+                    } else {
+                        w = range_weight_reg(P, rr[q] - rkj);
+                    }
+                }
                 v0 = v0 + w * c[q][0];
                 v1 = v1 + w * c[q][1];
                 v2 = v2 + w * c[q][2];
                 v3 = v3 + w * c[q][3];
             }
-            warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, v0, v1, v2, v3);
+            if constexpr (MODE == 1) {
+                warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, v0, v1, v2, v3);
+            } else {
+                warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, v0, v1, v2, v3);
+            }
             rkj = rkj + P.rdelta;
         }
     }
@@ -627,11 +650,12 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     pulse_body<MODE, PATH>(P, blockIdx.x, gridDim.x);
 }
 
-/* The plain pulse over a state in spatial order, K scatterers per lane
- * (PulseBins::add_k): warp w of block blk takes runs of 32 K neighbours. */
-template <int K>
+/* The plain or compensated pulse over a state in spatial order, K
+ * scatterers per lane (PulseBins::add_k): warp w of block blk takes runs of
+ * 32 K neighbours. */
+template <int MODE, int K>
 __global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
-    PulseBins<0, 1> B;
+    PulseBins<MODE, 1> B;
     B.init(P);
     const unsigned long long stride = (unsigned long long)K * gridDim.x * blockDim.x;
     const unsigned long long n = P.n;
