@@ -130,7 +130,13 @@ k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *pre
     if (threadIdx.x == 0) sp.pulse = out + (size_t)i * out_stride;
     __syncthreads();
     const unsigned b0 = __ldg(prefix + i);
-    pulse_body<MODE>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
+    /* an instance whose state is in spatial order takes two scatterers per
+     * lane, as the one-instance kernel does */
+    if (MODE != 2 && sp.coherent_span > 0 && !sp.materialize) {
+        pulse_body_group<MODE == 2 ? 0 : MODE, 2>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
+    } else {
+        pulse_body<MODE>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
+    }
 }
 
 }  // namespace rsc

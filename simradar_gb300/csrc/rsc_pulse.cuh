@@ -650,17 +650,16 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
     pulse_body<MODE, PATH>(P, blockIdx.x, gridDim.x);
 }
 
-/* The plain or compensated pulse over a state in spatial order, K
- * scatterers per lane (PulseBins::add_k): warp w of block blk takes runs of
- * 32 K neighbours. */
+/* Block blk of the nblk blocks forming one pulse, over a state in spatial
+ * order, K scatterers per lane (PulseBins::add_k): warp w of a block takes
+ * runs of 32 K neighbours. */
 template <int MODE, int K>
-__global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
+__device__ __forceinline__ void pulse_body_group(const PulseArgs &P, unsigned blk, unsigned nblk) {
     PulseBins<MODE, 1> B;
     B.init(P);
-    const unsigned long long stride = (unsigned long long)K * gridDim.x * blockDim.x;
+    const unsigned long long stride = (unsigned long long)K * nblk * blockDim.x;
     const unsigned long long n = P.n;
-    const unsigned long long base0 =
-        (unsigned long long)K * ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    const unsigned long long base0 = (unsigned long long)K * ((unsigned long long)blk * blockDim.x + (threadIdx.x & ~31u));
     for (unsigned long long base = base0; base < n; base += stride) {
         bool in[K];
         unsigned long long idx[K];
@@ -678,7 +677,14 @@ __global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
         }
         B.template add_k<K>(P, in, idx, pp, xx);
     }
-    B.finish(P, gridDim.x);
+    B.finish(P, nblk);
+}
+
+/* The plain or compensated pulse over a state in spatial order, K
+ * scatterers per lane. */
+template <int MODE, int K>
+__global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
+    pulse_body_group<MODE, K>(P, blockIdx.x, gridDim.x);
 }
 
 }  // namespace rsc
