@@ -559,10 +559,11 @@ struct PulseBins {
                         w = range_weight_reg(P, rr[q] - rkj);
                     }
                 }
-                v0 = v0 + w * c[q][0];
-                v1 = v1 + w * c[q][1];
-                v2 = v2 + w * c[q][2];
-                v3 = v3 + w * c[q][3];
+                /* fused: the lane's K terms of a gate in one rounding each */
+                v0 = fmaf(w, c[q][0], v0);
+                v1 = fmaf(w, c[q][1], v1);
+                v2 = fmaf(w, c[q][2], v2);
+                v3 = fmaf(w, c[q][3], v3);
             }
             if constexpr (MODE == 1) {
                 warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, v0, v1, v2, v3);

@@ -1,9 +1,11 @@
 """GPU parity: the sm_103a backend (through its C ABI) against the CPU oracle.
 
 State evolution (positions, velocities, orientations, tumbles, RCS, respawn
-seeds) must be bit-exact.  Pulses are sums of bit-identical per-scatterer,
-per-gate contributions taken in a different order, so they agree within the
-FP32 summation bound stated in PULSE_TOL below.
+seeds) must be bit-exact.  Pulses are sums over scatterers and gates of a
+bit-identical signal times a bit-identical gate weight, taken in a different
+order (and with the product fused into the running sum where the kernel
+holds two scatterers per lane), so they agree within the FP32 summation
+bound stated in PULSE_TOL below.
 """
 import numpy as np
 import pytest
