@@ -262,6 +262,50 @@ def test_small_and_ragged_sizes(backend, oracle_lib, n):
     W.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_non_finite_scatterers(backend, oracle_lib, precision):
+    """A scatterer with a non-finite backscatter reaches every gate, as in
+    make_pulse_pass_1 (0 x NaN is NaN): the values the oracle's exact sum
+    makes non-finite are non-finite on the GPU, in the caller's order and in
+    spatial order (the grouped kernel hands such warps to the one-scatterer
+    path), and every other value stays within the summation bound."""
+    O = oracle_lib
+    S = synth.make_scene(num_rain=20000, les_count=1, seed=77)
+    pop = synth.population(S)
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    W.set_precision(precision)
+    st = O.OracleState(S.state)
+    sd0 = synth.pulse_sim_desc(S, 0)
+    for sorted_state in (False, True):
+        if sorted_state:
+            W.advance_time(pop, 0, sd0)   # the first advance puts the state in spatial order
+            O.advance_time(st, S, S.counts, S.les[0], sd0)
+            assert W.sort_count >= 1
+        cur = W.download(("pos", "rcs"))
+        rcs, pos = cur["rcs"].copy(), cur["pos"].copy()
+        rcs[123, 0] = np.float32(np.nan)          # the H lanes of every gate
+        W.upload(0, rcs=rcs, pos=pos)
+        st.s["rcs"][:] = rcs
+        sd = synth.pulse_sim_desc(S, 3)
+        W.make_pulse(sd)
+        g = W.download_pulse(1.0)
+        direct, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+        where = "sorted" if sorted_state else "caller order"
+        assert np.array_equal(np.isfinite(g), np.isfinite(direct)), where
+        assert np.isnan(direct[:, :2]).all() and np.isfinite(direct[:, 2:]).all(), where
+        ok = np.isfinite(direct)
+        if precision == 0:
+            assert_pulse_close(np.where(ok, g, 0.0), np.where(ok, direct, 0.0), np.where(ok, ab, 0.0), where)
+        else:
+            r64, ab64 = O.make_pulse_f64(st, S, sd, return_abs=True)
+            assert_comp_close(np.where(ok, g, 0.0), np.where(ok, r64, 0.0), np.where(ok, ab64, 0.0), where)
+        rcs[123, 0] = np.float32(1.0)
+        W.upload(0, rcs=rcs)
+        st.s["rcs"][:] = rcs
+    W.close()
+
+
 def test_download_forms_sig_aux(backend, oracle_lib, scene_db):
     """RS_download returns aux / sig as scat_sig_aux wrote them (bit-exact),
     whether the pulse kernel wrote them or they are formed on download."""
