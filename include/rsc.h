@@ -176,9 +176,14 @@ int rsc_set_materialize_sig_aux(rsc_worker *w, int enable);
 /* Number of kernel launches this worker has issued (for accounting). */
 int rsc_launch_count(rsc_worker *w, uint64_t *count);
 
-/* The CUDA stream the worker issues on (as a void pointer, for callers that
- * time with events on it). */
+/* The CUDA stream the worker issues pulses and every other call on (as a
+ * void pointer, for callers that time with events on it).  Each call that
+ * reads the state first makes it wait for the advance stream. */
 int rsc_get_stream(rsc_worker *w, void **stream);
+/* The stream rsc_advance_time issues on, beside the pulse of the same step
+ * (the fused step form issues on the worker's stream instead).  Work queued
+ * on the worker's stream after a wait for this one sees every advance. */
+int rsc_get_advance_stream(rsc_worker *w, void **stream);
 
 /* ---- spatial order (additive) ----
  * The worker keeps its background scatterers (type 0) in Morton order of

@@ -32,6 +32,10 @@ struct DebrisType {
 };
 
 struct AdvanceArgs {
+    /* pos and rcs are read from pos_in / rcs_in and written to pos / rcs:
+     * the same arrays in place, or the worker's second pair so that the
+     * pulse of the same step can read the first pair meanwhile */
+    const float4 *pos_in, *rcs_in;
     float4 *pos, *vel, *ori, *tum, *rcs;
     uint4 *rnd;
     PairImage uvwt;
@@ -57,7 +61,7 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
     const uint32_t concept = __float_as_uint(sd[5]);
     const float rho_air = 1.225f;
     const float rho_over_mu_air = 6.7308e4f;
-    float4 pos = a.pos[i];
+    float4 pos = a.pos_in[i];
     float4 vel = a.vel[i];
     pos.x = fmaf(vel.x, dt, pos.x);
     pos.y = fmaf(vel.y, dt, pos.y);
@@ -75,6 +79,7 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
         a.pos[i] = pos;
         a.vel[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
         a.rnd[i] = seed;
+        if (a.rcs != a.rcs_in) a.rcs[i] = a.rcs_in[i];
         po = pos;
         xk = false;
         return;
@@ -117,7 +122,7 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
 __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const float dt = sd[11];
-    float4 pos = a.pos[i];
+    float4 pos = a.pos_in[i];
     float4 vel = a.vel[i];
     pos.x = pos.x + vel.x * dt;
     pos.y = pos.y + vel.y * dt;
@@ -132,6 +137,7 @@ __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &
         a.pos[i] = pos;
         a.vel[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
         a.rnd[i] = seed;
+        if (a.rcs != a.rcs_in) a.rcs[i] = a.rcs_in[i];
         po = pos;
         xk = false;
         return;
@@ -151,9 +157,9 @@ __device__ __forceinline__ void rain_fp(const AdvanceArgs &a, size_t i, float4 &
     const float *sd = a.sim;
     const float wav_num = sd[4];
     const float dt = sd[11];
-    float4 pos = a.pos[i];
+    float4 pos = a.pos_in[i];
     float4 vel = a.vel[i];
-    float4 rcs = a.rcs[i];
+    float4 rcs = a.rcs_in[i];
     float c3[3];
     wind_table_index(c3, pos, a.wind, sd);
     float4 uv = read_pair_image3d(a.uvwt, c3[0], c3[1], c3[2]);
@@ -174,6 +180,7 @@ __device__ __forceinline__ void rain_fp(const AdvanceArgs &a, size_t i, float4 &
     vel.z = uv.z;
     a.vel[i] = vel;
     a.rcs[i] = rcs;
+    if (a.pos != a.pos_in) a.pos[i] = pos;   /* fp_atts leaves the position */
     po = pos;
     xo = rcs;
     xk = true;
@@ -184,7 +191,7 @@ __device__ __forceinline__ void debris_step(const AdvanceArgs &a, const DebrisTy
     const float *sd = a.sim;
     const uint32_t concept = __float_as_uint(sd[5]);
     const float dt = sd[11];
-    float4 pos = a.pos[i];
+    float4 pos = a.pos_in[i];
     float4 ori = a.ori[i];
     float4 vel = a.vel[i];
     float4 tum = a.tum[i];
@@ -316,7 +323,7 @@ __device__ __forceinline__ bool advance_one_t(const AdvanceArgs &a, unsigned b, 
         } else {
             rain_fp(a, i, pos, rcs, known);
         }
-        if (!known) rcs = a.rcs[i];   /* respawned: the stored backscatter stays */
+        if (!known) rcs = a.rcs_in[i];   /* respawned: the stored backscatter stays */
         i_out = i;
         return true;
     }

@@ -93,16 +93,17 @@ def load_library():
         "rsc_set_dff": ([P, I, _f32p, U32, _f32p], I),
         "rsc_upload": ([P, S, S, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _u32p], I),
         "rsc_download": ([P, S, S, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _u32p], I),
-        "rsc_advance_time": ([P, ctypes.POINTER(Population), I, _f32p], I),
+        "rsc_advance_time": ([P, ctypes.POINTER(Population), I, P], I),
         "rsc_update_debris_rcs": ([P, ctypes.POINTER(Population), _f32p], I),
-        "rsc_make_pulse": ([P, _f32p], I),
-        "rsc_download_pulse": ([P, _f32p, F], I),
+        "rsc_make_pulse": ([P, P], I),
+        "rsc_download_pulse": ([P, P, F], I),
         "rsc_synchronize": ([P], I),
-        "rsc_download_pulse_async": ([P, _f32p], I),
+        "rsc_download_pulse_async": ([P, P], I),
         "rsc_set_pulse_precision": ([P, I], I),
         "rsc_set_materialize_sig_aux": ([P, I], I),
         "rsc_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
         "rsc_get_stream": ([P, ctypes.POINTER(P)], I),
+        "rsc_get_advance_stream": ([P, ctypes.POINTER(P)], I),
         "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
         "rsc_autotune": ([P, _f32p, ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "rsc_set_sort_interval": ([P, I], I),
@@ -151,6 +152,13 @@ def _up(a):
 
 def f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _addr(a):
+    """Address of a C-contiguous float32 array (the per-pulse calls take
+    plain addresses: cheaper than a ctypes pointer object)."""
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"], "expected C-contiguous float32"
+    return a.ctypes.data
 
 
 def device_count():
@@ -284,7 +292,7 @@ class Worker:
     # --- hot path --------------------------------------------------------
     def advance_time(self, pop, les_id, sim_desc):
         d = f32(sim_desc)
-        _check(self._lib.rsc_advance_time(self._h, ctypes.byref(pop), int(les_id), _fp(d)))
+        _check(self._lib.rsc_advance_time(self._h, ctypes.byref(pop), int(les_id), _addr(d)))
 
     def update_debris_rcs(self, pop, sim_desc):
         d = f32(sim_desc)
@@ -292,12 +300,12 @@ class Worker:
 
     def make_pulse(self, sim_desc):
         d = f32(sim_desc)
-        _check(self._lib.rsc_make_pulse(self._h, _fp(d)))
+        _check(self._lib.rsc_make_pulse(self._h, _addr(d)))
 
     def download_pulse(self, gain=1.0, out=None):
         if out is None:
             out = np.empty((self.range_count, 4), dtype=np.float32)
-        _check(self._lib.rsc_download_pulse(self._h, _fp(out), float(gain)))
+        _check(self._lib.rsc_download_pulse(self._h, _addr(out), float(gain)))
         return out
 
     def download_pulse_async(self, out):
@@ -305,7 +313,7 @@ class Worker:
         (range_count, 4) float32 array (page-locked for an asynchronous
         copy); it is complete after synchronize()."""
         assert out.shape == (self.range_count, 4)
-        _check(self._lib.rsc_download_pulse_async(self._h, _fp(out)))
+        _check(self._lib.rsc_download_pulse_async(self._h, _addr(out)))
 
     def synchronize(self):
         _check(self._lib.rsc_synchronize(self._h))
@@ -326,6 +334,13 @@ class Worker:
     def stream(self):
         s = ctypes.c_void_p()
         _check(self._lib.rsc_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    @property
+    def advance_stream(self):
+        """The stream advance_time issues on, beside the pulses."""
+        s = ctypes.c_void_p()
+        _check(self._lib.rsc_get_advance_stream(self._h, ctypes.byref(s)))
         return s.value or 0
 
     def set_sort_interval(self, steps):
