@@ -169,12 +169,21 @@ __device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4
     /* attenuation 1 / r^2 from the double-float r^2 */
     const float inv = 1.0f / r2h;
     const float atten = fmaf(-inv, r2l * inv, inv);
-    const float ms = -ss;
-    o.sig[0] = fmaf(x.x, cc, -(x.y * ms)) * atten;
-    o.sig[1] = fmaf(x.y, cc, x.x * ms) * atten;
-    o.sig[2] = fmaf(x.z, cc, -(x.w * ms)) * atten;
-    o.sig[3] = fmaf(x.w, cc, x.z * ms) * atten;
-    o.s.set(o.sig[0] * o.wang, o.sig[1] * o.wang, o.sig[2] * o.wang, o.sig[3] * o.wang);
+    /* the rotation a cc + b ss with the product b ss exact (its rounding
+     * error folded back by an FMA), then one product by atten * wang */
+    const float k = atten * o.wang;
+    float rot[4];
+    const float xa[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        const float a = xa[l], b = (l & 1) ? -xa[l - 1] : xa[l + 1];   /* (x.x, x.y) -> x.x cc + x.y ss, x.y cc - x.x ss */
+        const float p = b * ss;
+        const float pe = fmaf(b, ss, -p);
+        rot[l] = fmaf(a, cc, p) + pe;
+    }
+#pragma unroll
+    for (int l = 0; l < 4; l++) o.sig[l] = rot[l] * atten;
+    o.s.set(rot[0] * k, rot[1] * k, rot[2] * k, rot[3] * k);
     o.r = rh;
     o.r_lo = rl;
 }
