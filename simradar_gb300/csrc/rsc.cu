@@ -1639,6 +1639,10 @@ struct rsc_batch {
     /* the debris kernel beside the background kernel (high priority) */
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev = nullptr, side_ev = nullptr;
+    /* the advance stream (the pulse of a step runs on `stream` beside it):
+     * ev_bp / ev_ba after the pulse / advance of the last two steps */
+    cudaStream_t adv = nullptr;
+    cudaEvent_t ev_bp[2] = {nullptr, nullptr}, ev_ba[2] = {nullptr, nullptr}, ev_afork = nullptr;
     std::vector<rsc_worker *> w;
     std::vector<rsc_population> pops;
     bool have_pops = false;
@@ -1813,16 +1817,38 @@ cudaError_t batch_launch_pulse(rsc_batch *b, int k) {
     return cudaGetLastError();
 }
 
-/* Steps 0..K-1: pulse of every instance, then the advance of every instance
- * (background kernel on the batch's stream, debris kernel beside it). */
+/* Steps 0..K-1: the pulse of every instance on the batch's stream and the
+ * advance of every instance beside it on the advance stream (background
+ * kernel, debris kernel on the side stream).  The pulse of step k waits for
+ * the advance of step k - 1 (which wrote what it reads); the advance of step
+ * k for the pulse of step k - 1 (which read the pair it overwrites).  The
+ * advance stream starts after the work queued on the batch's stream and the
+ * batch's stream ends after it. */
 cudaError_t batch_enqueue(rsc_batch *b, int steps) {
     const int n = (int)b->w.size();
-    for (int k = 0; k < steps; k++) {
-        cudaError_t e = batch_launch_pulse(b, k);
+    const bool advance = b->rain_blocks || b->deb_blocks;
+    cudaError_t e = cudaSuccess;
+    if (advance) {
+        e = cudaEventRecord(b->ev_afork, b->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->adv, b->ev_afork, 0);
         if (e != cudaSuccess) return e;
+    }
+    for (int k = 0; k < steps; k++) {
+        if (advance && k > 0) {
+            e = cudaStreamWaitEvent(b->stream, b->ev_ba[(k - 1) & 1], 0);
+            if (e != cudaSuccess) return e;
+        }
+        e = batch_launch_pulse(b, k);
+        if (e == cudaSuccess && advance) e = cudaEventRecord(b->ev_bp[k & 1], b->stream);
+        if (e != cudaSuccess) return e;
+        if (!advance) continue;
         const rsc::BatchStep *st = b->d_steps + (size_t)k * n;
+        if (k > 0) {
+            e = cudaStreamWaitEvent(b->adv, b->ev_bp[(k - 1) & 1], 0);
+            if (e != cudaSuccess) return e;
+        }
         if (b->deb_blocks) {
-            e = cudaEventRecord(b->fork_ev, b->stream);
+            e = cudaEventRecord(b->fork_ev, b->adv);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork_ev, 0);
             if (e != cudaSuccess) return e;
             rsc::k_advance_batch_debris<<<b->deb_blocks, rsc::kAdvanceThreads, 0, b->side>>>(b->d_adv, st,
@@ -1832,17 +1858,20 @@ cudaError_t batch_enqueue(rsc_batch *b, int steps) {
             if (e != cudaSuccess) return e;
         }
         if (b->rain_blocks) {
-            rsc::k_advance_batch_rain<<<b->rain_blocks, rsc::kAdvanceThreads, 0, b->stream>>>(b->d_adv, st,
-                                                                                             b->d_rain_prefix, n);
+            rsc::k_advance_batch_rain<<<b->rain_blocks, rsc::kAdvanceThreads, 0, b->adv>>>(b->d_adv, st,
+                                                                                          b->d_rain_prefix, n);
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
         if (b->deb_blocks) {
-            e = cudaStreamWaitEvent(b->stream, b->side_ev, 0);
+            e = cudaStreamWaitEvent(b->adv, b->side_ev, 0);
             if (e != cudaSuccess) return e;
         }
+        e = cudaEventRecord(b->ev_ba[k & 1], b->adv);
+        if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    if (advance) e = cudaStreamWaitEvent(b->stream, b->ev_ba[(steps - 1) & 1], 0);
+    return e;
 }
 
 int batch_capture(rsc_batch *b, int steps) {
@@ -1860,6 +1889,36 @@ int batch_capture(rsc_batch *b, int steps) {
     }
     b->graph_steps = steps;
     return RSC_OK;
+}
+
+/* The pos / rcs pairs of every step: step k of a run reads the instance's
+ * current pair when k is even, its other pair when k is odd, and the advance
+ * writes the other one. */
+void batch_fill_pairs(rsc_batch *b, int steps) {
+    const size_t n = b->w.size();
+    for (int k = 0; k < steps; k++) {
+        for (size_t i = 0; i < n; i++) {
+            rsc_worker *x = b->w[i];
+            rsc::BatchStep &S = b->h_steps[(size_t)k * n + i];
+            const bool odd = (k & 1) != 0;
+            S.pos_r = odd ? x->pos_next : x->pos;
+            S.rcs_r = odd ? x->rcs_next : x->rcs;
+            S.pos_w = odd ? x->pos : x->pos_next;
+            S.rcs_w = odd ? x->rcs : x->rcs_next;
+        }
+    }
+}
+
+/* After a run of `steps` steps: an odd count leaves each instance's state in
+ * its other pair. */
+void batch_swap_pairs(rsc_batch *b, int steps) {
+    if ((steps & 1) == 0 || (b->rain_blocks == 0 && b->deb_blocks == 0)) return;
+    for (rsc_worker *x : b->w) {
+        std::swap(x->pos, x->pos_next);
+        std::swap(x->rcs, x->rcs_next);
+        std::swap(x->ev_read, x->ev_read_next);
+        std::swap(x->read_pending, x->read_next_pending);
+    }
 }
 
 /* Copy steps' descriptors into the pinned table, checking them. */
@@ -1982,16 +2041,25 @@ int rsc_batch_create(rsc_worker *const *workers, int count, rsc_batch **out) {
     b->pops.assign(count, rsc_population());
     for (rsc_worker *x : b->w) b->Gmax = x->G > b->Gmax ? x->G : b->Gmax;
     cudaError_t e = cudaSetDevice(b->device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    /* priorities as a worker's: pulses ahead of the background advance,
+     * debris ahead of both */
+    int prio_least = 0, prio_greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    const int prio_main = prio_greatest < prio_least ? prio_greatest + 1 : prio_greatest;
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, prio_main);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_h2d, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking);
-    int prio_least = 0, prio_greatest = 0;
-    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, prio_greatest);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->side_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->adv, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        e = cudaEventCreateWithFlags(&b->ev_bp[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_ba[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_afork, cudaEventDisableTiming);
     b->slot_used.assign(2 * count, nullptr);
     b->slot_ready.assign(2 * count, nullptr);
     b->slot_pending.assign(2 * count, 0);
@@ -2040,6 +2108,15 @@ int rsc_batch_free(rsc_batch *b) {
     }
     if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     if (b->side_ev) cudaEventDestroy(b->side_ev);
+    if (b->adv) {
+        cudaStreamSynchronize(b->adv);
+        cudaStreamDestroy(b->adv);
+    }
+    for (int k = 0; k < 2; k++) {
+        if (b->ev_bp[k]) cudaEventDestroy(b->ev_bp[k]);
+        if (b->ev_ba[k]) cudaEventDestroy(b->ev_ba[k]);
+    }
+    if (b->ev_afork) cudaEventDestroy(b->ev_afork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
     if (b->ev_h2d) cudaEventDestroy(b->ev_h2d);
     if (b->ev_done) cudaEventDestroy(b->ev_done);
@@ -2082,6 +2159,7 @@ int rsc_batch_autotune(rsc_batch *b, const float *sim_descs) {
     s = batch_join_workers(b);
     if (s) return s;
     const size_t n = b->w.size();
+    batch_fill_pairs(b, 1);
     RSC_CUDA(cudaMemcpyAsync(b->d_steps, b->h_steps, n * sizeof(rsc::BatchStep), cudaMemcpyHostToDevice, b->stream));
     RSC_CUDA(cudaEventRecord(b->ev_h2d, b->stream));
     EventPair ev;
@@ -2138,9 +2216,14 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
     for (size_t i = 0; i < n; i++) {
         s = maybe_sort(b->w[i], &b->pops[i], b->h_steps[i].sim, b->stream);
         if (s) return s;
+        /* the advances write both pairs: scatterers outside the population
+         * ranges carry over into the other one */
+        s = copy_unadvanced(b->w[i], &b->pops[i], b->stream);
+        if (s) return s;
     }
     s = batch_prepare(b, b->h_steps);
     if (s) return s;
+    batch_fill_pairs(b, steps);
     /* LES slots this run reads: wait for their pending refills */
     std::vector<char> used(2 * n, 0);
     for (size_t r = 0; r < (size_t)steps * n; r++) used[2 * (r % n) + (b->h_steps[r].les_id & 1)] = 1;
@@ -2169,6 +2252,7 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
         RSC_CUDA(batch_enqueue(b, steps));
     }
     b->launches += (uint64_t)steps * (1u + (b->rain_blocks ? 1u : 0u) + (b->deb_blocks ? 1u : 0u));
+    batch_swap_pairs(b, steps);
     for (size_t q = 0; q < 2 * n; q++) {
         if (used[q]) RSC_CUDA(cudaEventRecord(b->slot_used[q], b->stream));
     }

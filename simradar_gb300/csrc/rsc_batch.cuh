@@ -3,9 +3,11 @@
  *
  * An instance is one worker: its own scatterer arrays, tables, gates, pulse
  * accumulator and counter.  One time step of every instance is three
- * launches: k_pulse_batch forms every instance's pulse, k_advance_batch_rain
- * advances every instance's background range and k_advance_batch_debris,
- * beside it on a high-priority stream, every instance's debris.  Blocks are assigned to instances in proportion to
+ * launches: k_pulse_batch forms every instance's pulse on the batch's
+ * stream while k_advance_batch_rain advances every instance's background
+ * range on the advance stream (into the instance's other pos / rcs pair) and
+ * k_advance_batch_debris, beside it on a high-priority stream, every
+ * instance's debris.  Blocks are assigned to instances in proportion to
  * their work through a prefix table; each block copies its instance's launch
  * descriptor into shared memory, takes the step's beam / time / LES slot from
  * the per-step table, and runs the same block bodies as the one-instance
@@ -20,11 +22,16 @@
 
 namespace rsc {
 
-/* per instance per step: the simulation descriptor and the LES slot */
+/* per instance per step: the simulation descriptor, the LES slot, and the
+ * pos / rcs pair the step's pulse and advance read and the pair the advance
+ * writes (the instance's two pairs alternate from step to step, so the
+ * pulse of a step runs beside its advance) */
 struct BatchStep {
     float sim[16];
     int les_id;
     int pad[3];
+    const float4 *pos_r, *rcs_r;
+    float4 *pos_w, *rcs_w;
 };
 
 /* per instance, fixed for the batch: the advance descriptor plus both LES /
@@ -72,6 +79,10 @@ __device__ __forceinline__ int batch_advance_args(AdvanceArgs &sa, int &s_i, con
         sa.uvwt = inst[i].uvwt[les];
         sa.cpxx = inst[i].cpxx[les];
         sa.dff = inst[i].dff[les];
+        sa.pos_in = steps[i].pos_r;
+        sa.rcs_in = steps[i].rcs_r;
+        sa.pos = steps[i].pos_w;
+        sa.rcs = steps[i].rcs_w;
     }
     __syncthreads();
     return i;
@@ -127,7 +138,11 @@ k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *pre
     block_copy(&sp, &inst[i], sizeof(PulseArgs));
     __syncthreads();
     if (threadIdx.x < 16) sp.sim[threadIdx.x] = steps[i].sim[threadIdx.x];
-    if (threadIdx.x == 0) sp.pulse = out + (size_t)i * out_stride;
+    if (threadIdx.x == 0) {
+        sp.pulse = out + (size_t)i * out_stride;
+        sp.pos = steps[i].pos_r;
+        sp.rcs = steps[i].rcs_r;
+    }
     __syncthreads();
     const unsigned b0 = __ldg(prefix + i);
     /* an instance whose state is in spatial order takes two scatterers per

@@ -209,3 +209,51 @@ def test_batch_errors(backend, scenes):
     B.close()
     for W in ws:
         W.close()
+
+
+def test_partial_population_batch_and_worker(backend, oracle_lib):
+    """Scatterers outside the population (here the last debris type) keep
+    their position and backscatter while the others advance into the other
+    pos / rcs pair, and they still take part in every pulse: batch runs of an
+    odd step count interleaved with one-worker steps on the advance stream,
+    with spatial sorts between them."""
+    O = oracle_lib
+    S = synth.make_scene(num_rain=6000, debris=[(synth.OBJ_LEAF, 256), (synth.OBJ_WOODBOARD_2X4, 256),
+                                                (synth.OBJ_BRICK, 256)], les_count=1, seed=21)
+    push_to_edges(S)
+    counts = list(S.counts)
+    counts[-1] = 0
+    pop = backend.Population.make(counts)
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    W.set_sort_interval(2)
+    B = backend.Batch([W])
+    B.set_populations([pop])
+    st = O.OracleState(S.state)
+    k = 0
+
+    def check_pulse(g, sd, where):
+        direct, ab = O.make_pulse_direct(st, S, sd, return_abs=True)
+        assert np.isfinite(g).all()
+        assert_pulse_close(g, direct, ab, where)
+
+    for rnd in range(2):
+        sims = np.stack([synth.pulse_sim_desc(S, k + j, tic=(k + j) * 1e-3) for j in range(3)])[:, None, :]
+        pulses = B.run(sims, np.zeros((3, 1), np.int32), use_graph=rnd == 1)
+        for j in range(3):
+            check_pulse(pulses[j, 0, :S.range_count], sims[j, 0], "batch step %d" % (k + j))
+            O.advance_time(st, S, counts, S.les[0], sims[j, 0])
+        k += 3
+        for _ in range(2):
+            sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+            W.make_pulse(sd)
+            check_pulse(W.download_pulse(1.0), sd, "worker step %d" % k)
+            W.advance_time(pop, 0, sd)
+            O.advance_time(st, S, counts, S.les[0], sd)
+            k += 1
+        assert_state_equal(W.download(STATE_FIELDS), st.s, where="after step %d " % (k - 1))
+    # the last type never moved
+    lo = sum(counts)
+    assert np.array_equal(bits(st.s["pos"][lo:]), bits(S.state["pos"][lo:]))
+    B.close()
+    W.close()

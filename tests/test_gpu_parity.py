@@ -429,8 +429,9 @@ def test_download_pulse_async(backend, scene_db):
 def test_download_pulse_async_queued(backend, scene_db):
     """Pulses copied asynchronously into page-locked buffers while the host
     queues the following steps: each buffer holds its own step's pulse (the
-    next pulse kernel waits for the copy), compared with a second worker that
-    reads every pulse with a blocking download."""
+    next pulse kernel waits for the copy) and the state ends bit-identical,
+    compared with a second worker that reads every pulse with a blocking
+    download (no overlap between its steps)."""
     torch = pytest.importorskip("torch")
     S = scene_db
     pop = synth.population(S)
@@ -453,6 +454,9 @@ def test_download_pulse_async_queued(backend, scene_db):
         scale = float(np.abs(refs[k]).max())
         assert scale > 0.0
         np.testing.assert_allclose(ring[k], refs[k], rtol=1e-4, atol=1e-5 * scale, err_msg=str(k))
+    # the queued steps (pulses and advances overlapping on their two
+    # streams) leave the same state as the stepped ones
+    assert_state_equal(A.download(STATE_FIELDS), B.download(STATE_FIELDS), where="queued vs stepped ")
     A.close()
     B.close()
 
