@@ -216,6 +216,12 @@ int rsc_set_fused_step(rsc_worker *w, int enable);
  * keep the fastest for later rsc_make_pulse calls.  sim_desc is the beam to
  * time with; the state is not changed (the pulse is recomputed). */
 int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *blocks_per_sm_out);
+/* Set the pulse kernel's shape directly: warps per block (1-16) and resident
+ * blocks per SM (1-4), each capped by what the kernel's shared memory and
+ * registers allow; 0 for either returns to the largest that fits.  Fewer
+ * pulse blocks per SM leave room for the advance of the same step, which
+ * runs beside the pulse on the advance stream. */
+int rsc_set_pulse_shape(rsc_worker *w, int warps, int blocks_per_sm);
 
 /* ---- batching form (additive; no counterpart in rs.c) ----
  * A batch runs many emulation instances -- each an rsc_worker with its own

@@ -1966,6 +1966,17 @@ int batch_join_workers(rsc_batch *b) {
 
 extern "C" {
 
+int rsc_set_pulse_shape(rsc_worker *w, int warps, int blocks_per_sm) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (warps < 0 || warps > 16 || blocks_per_sm < 0 || blocks_per_sm > 4) {
+        return fail(RSC_ERR_ARG, "pulse shape %d warps x %d blocks per SM", warps, blocks_per_sm);
+    }
+    w->tune_warps = warps;
+    w->tune_per_sm = blocks_per_sm;
+    return RSC_OK;
+}
+
 int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *blocks_per_sm_out) {
     int s = check_alloc(w);
     if (s) return s;

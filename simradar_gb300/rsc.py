@@ -106,6 +106,7 @@ def load_library():
         "rsc_get_advance_stream": ([P, ctypes.POINTER(P)], I),
         "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
         "rsc_autotune": ([P, _f32p, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "rsc_set_pulse_shape": ([P, I, I], I),
         "rsc_set_sort_interval": ([P, I], I),
         "rsc_set_fused_step": ([P, I], I),
         "rsc_sort_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
@@ -364,6 +365,10 @@ class Worker:
         wv, pv = ctypes.c_int(0), ctypes.c_int(0)
         _check(self._lib.rsc_autotune(self._h, _fp(d), ctypes.byref(wv), ctypes.byref(pv)))
         return wv.value, pv.value
+
+    def set_pulse_shape(self, warps, blocks_per_sm):
+        """Fix the pulse kernel's launch shape (0 = the largest that fits)."""
+        _check(self._lib.rsc_set_pulse_shape(self._h, int(warps), int(blocks_per_sm)))
 
 
 class Batch:

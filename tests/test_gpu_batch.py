@@ -181,6 +181,14 @@ def test_worker_autotune(backend, scenes):
     W.make_pulse(sd)
     g = W.download_pulse(1.0)
     assert np.all(np.abs(g - ref) <= 1e-4 * np.abs(ref).max())
+    # shapes set by hand (one warp per block up to the largest that fits)
+    for shape in ((1, 1), (8, 3), (16, 4), (0, 0)):
+        W.set_pulse_shape(*shape)
+        W.make_pulse(sd)
+        g = W.download_pulse(1.0)
+        assert np.all(np.abs(g - ref) <= 1e-4 * np.abs(ref).max()), shape
+    with pytest.raises(backend.BackendError):
+        W.set_pulse_shape(17, 1)
     assert_state_equal(W.download(STATE_FIELDS), S.state, where="after autotune ")
     W.close()
 
