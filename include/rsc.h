@@ -227,9 +227,11 @@ int rsc_set_pulse_shape(rsc_worker *w, int warps, int blocks_per_sm);
  * A batch runs many emulation instances -- each an rsc_worker with its own
  * state, tables, gates, concept and population, all on one device -- one
  * time step at a time, with three launches per step for all of them (the
- * pulse, then the background advance and, beside it on a high-priority
- * stream, the debris advance: the order of simradar's loop,
- * simradar.c:1032-1070).  Each instance evolves exactly as it would alone. */
+ * pulse, and beside it on a second stream the background advance and, on a
+ * high-priority stream, the debris advance: the order of simradar's loop,
+ * simradar.c:1032-1070, with the advance writing each instance's second
+ * pos / rcs pair while the pulse reads the first).  Each instance evolves
+ * exactly as it would alone. */
 typedef struct rsc_batch rsc_batch;
 
 /* The workers must be allocated and have their tables set.  The batch keeps
