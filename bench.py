@@ -352,30 +352,9 @@ def bench_precision(torch, rsc, synth, dev, steps):
 
 
 # ---------------------------------------------------------------------- batch
-def batch_scenes(synth, count, seed=2024):
-    rng = np.random.default_rng(seed)
-    sizes = np.exp(rng.uniform(math.log(65536), math.log(4194304), count)).astype(np.int64)
-    deb = rng.integers(0, 4097, size=(count, 3))
-    n0 = rng.uniform(4000.0, 16000.0, count)
-    base = synth.make_scene(num_rain=1, les_count=1, with_tables=True)
-    scenes = []
-    for i in range(count):
-        if i % 2 == 0:
-            scan = synth.ppi_positions(float(rng.uniform(1.0, 6.0)), -12.0, 12.0, 0.24)
-        else:
-            scan = synth.rhi_positions(float(rng.uniform(-6.0, 6.0)), 0.5, 20.0, 0.2)
-        debris = [(o, int(c)) for o, c in zip((synth.OBJ_LEAF, synth.OBJ_WOODBOARD_2X4, synth.OBJ_BRICK), deb[i])
-                  if c > 0]
-        S = synth.make_scene(num_rain=int(sizes[i]), debris=debris, gates=GATES, les_count=1, with_tables=False,
-                             seed=1000 + i, scan=scan, dsd_n0=float(n0[i]))
-        S.les, S.les_cfg, S.les_desc = base.les, base.les_cfg, base.les_desc
-        scenes.append(S)
-    return scenes
-
-
 def bench_batch(torch, rsc, synth, dev, steps):
     count = 64
-    scenes = batch_scenes(synth, count)
+    scenes = synth.batch_workload(count, gates=GATES)
     ws = []
     for S in scenes:
         W = rsc.Worker(dev)

@@ -521,3 +521,27 @@ def load_worker(W, S, les_slot_volumes=(0, 1)):
     for t, (re, im, rd) in enumerate(S.rcs_tables):
         W.set_rcs(t, re, im, rd)
     W.upload(0, **S.state)
+
+
+def batch_workload(count=64, seed=2024, gates=40):
+    """The batching workload: `count` instances with scatterer counts
+    log-uniform in [65,536, 4,194,304], 0-4096 debris of each of leaf, 2x4
+    board and brick, Marshall-Palmer N0 uniform in [4000, 16000], PPI (even
+    instances) and RHI (odd) scans, one LES volume shared by all."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(65536), math.log(4194304), count)).astype(np.int64)
+    deb = rng.integers(0, 4097, size=(count, 3))
+    n0 = rng.uniform(4000.0, 16000.0, count)
+    base = make_scene(num_rain=1, les_count=1, with_tables=True)
+    scenes = []
+    for i in range(count):
+        if i % 2 == 0:
+            scan = ppi_positions(float(rng.uniform(1.0, 6.0)), -12.0, 12.0, 0.24)
+        else:
+            scan = rhi_positions(float(rng.uniform(-6.0, 6.0)), 0.5, 20.0, 0.2)
+        debris = [(o, int(c)) for o, c in zip((OBJ_LEAF, OBJ_WOODBOARD_2X4, OBJ_BRICK), deb[i]) if c > 0]
+        S = make_scene(num_rain=int(sizes[i]), debris=debris, gates=gates, les_count=1, with_tables=False,
+                       seed=1000 + i, scan=scan, dsd_n0=float(n0[i]))
+        S.les, S.les_cfg, S.les_desc = base.les, base.les_cfg, base.les_desc
+        scenes.append(S)
+    return scenes

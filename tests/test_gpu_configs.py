@@ -10,7 +10,8 @@ through the C ABI against the oracle:
   the plain pulse against the reference's order and the compensated pulse
   against the FP64 pulse of the same state;
 * 33,554,432 rain + 131,072 debris on a 352 x 352 x 160 LES, RHI, as a
-  batch of one in the compensated form.
+  batch of one in the compensated form;
+* the 64-instance batching workload (synth.batch_workload).
 """
 import numpy as np
 import pytest
@@ -94,3 +95,37 @@ def test_33m_batch_of_one(backend, oracle_lib):
     assert_state_equal(W.download(STATE_FIELDS), st.s, where="after two steps ")
     B.close()
     W.close()
+
+
+def test_64_instances_batched(backend, oracle_lib):
+    """The batching workload (64 instances, 53.5 M scatterers in all, sizes
+    log-uniform 65,536-4,194,304, PPI / RHI mix), compensated, one graph run
+    of two steps: every instance's state bit-exact, every pulse against its
+    FP64 pulse."""
+    O = oracle_lib
+    scenes = synth.batch_workload(64)
+    ws, sts = [], []
+    for S in scenes:
+        W = backend.Worker(0)
+        synth.load_worker(W, S)
+        ws.append(W)
+        sts.append(O.OracleState(S.state))
+        S.state = None
+    B = backend.Batch(ws)
+    B.set_populations([synth.population(S) for S in scenes])
+    B.set_precision(1)
+    steps = 2
+    sims = np.zeros((steps, len(scenes), 16), np.float32)
+    for j in range(steps):
+        for i, S in enumerate(scenes):
+            sims[j, i] = synth.pulse_sim_desc(S, j, tic=j * 1e-3)
+    pulses = B.run(sims, np.zeros((steps, len(scenes)), np.int32), use_graph=True)
+    for i, S in enumerate(scenes):
+        for j in range(steps):
+            r64, ab = O.make_pulse_f64(sts[i], S, sims[j, i], return_abs=True)
+            assert_comp_close(pulses[j, i, :S.range_count], r64, ab, "instance %d step %d" % (i, j))
+            O.advance_time(sts[i], S, S.counts, S.les[0], sims[j, i])
+        assert_state_equal(ws[i].download(STATE_FIELDS), sts[i].s, where="instance %d " % i)
+    B.close()
+    for W in ws:
+        W.close()
