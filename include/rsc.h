@@ -286,7 +286,9 @@ int rsc_batch_max_gates(rsc_batch *b, int *max_gates);
  * background and the debris advance where the batch has such scatterers,
  * plus the autotuner's). */
 int rsc_batch_launch_count(rsc_batch *b, uint64_t *count);
-/* The CUDA stream the batch issues on. */
+/* The CUDA stream the batch issues on.  A run's advances run on streams of
+ * its own, forked from this one at the run's start and joined back into it
+ * before the run's end, so work queued here after a run sees all of it. */
 int rsc_batch_get_stream(rsc_batch *b, void **stream);
 /* The pulse shape chosen by rsc_batch_autotune (0, 0 before it runs). */
 int rsc_batch_get_shape(rsc_batch *b, int *warps, int *blocks_per_sm);
