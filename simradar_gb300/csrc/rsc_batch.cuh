@@ -89,11 +89,11 @@ __device__ __forceinline__ int batch_advance_args(AdvanceArgs &sa, int &s_i, con
 }
 
 /* The background range of every instance (prefix over their background
- * blocks); the rain body chosen per instance by its concept.  8 resident
- * blocks per SM (32 registers, 76 bytes spilled) measured 6% faster per
- * batched step than 6 blocks (40 registers), which had been faster than 5:
- * resident warps hide the texel loads' latency. */
-__global__ void __launch_bounds__(kAdvanceThreads, 8)
+ * blocks); the rain body chosen per instance by its concept.  A full SM of
+ * resident threads (32 registers, 76 bytes spilled) measured 6% faster per
+ * batched step than 6 blocks of 256 (40 registers), which had been faster
+ * than 5: resident warps hide the texel loads' latency. */
+__global__ void __launch_bounds__(kAdvanceThreads, 2048 / kAdvanceThreads)
 k_advance_batch_rain(const BatchAdvance *inst, const BatchStep *steps, const unsigned *prefix, int ninst) {
     __shared__ __align__(16) AdvanceArgs sa;
     __shared__ int s_i;

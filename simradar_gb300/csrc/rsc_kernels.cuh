@@ -21,7 +21,7 @@
 
 namespace rsc {
 
-constexpr int kAdvanceThreads = 256;
+constexpr int kAdvanceThreads = 128;
 constexpr int kMaxCandidates = 8;
 
 struct DebrisType {
@@ -345,13 +345,15 @@ __device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, un
 /* One time step as two kernels: the background kernel holds only its own
  * (short) path, which the debris path's code slows by about a tenth when both
  * share one kernel; the host runs the debris kernel beside it on a second,
- * high-priority stream.  8 blocks of 256 per SM (32 registers, a few bytes
+ * high-priority stream.  16 blocks of 128 per SM (32 registers, a few bytes
  * spilled in el_atts): the step is a chain of dependent loads (state, then
  * the LES texel pairs), so resident warps are what hides the latency (2.4%
- * faster per step than 6 blocks at 40 registers).  The fused step kernel
- * takes both paths through advance_one. */
+ * faster per step than 6 blocks of 256 at 40 registers), and blocks of 128
+ * fill the SM slots the pulse of the same step leaves another 2.3% faster
+ * than blocks of 256.  The fused step kernel takes both paths through
+ * advance_one. */
 template <int RAIN_MODE>
-__global__ void __launch_bounds__(kAdvanceThreads, 8) k_advance_rain(const AdvanceArgs a) {
+__global__ void __launch_bounds__(kAdvanceThreads, 2048 / kAdvanceThreads) k_advance_rain(const AdvanceArgs a) {
     const unsigned long long j = (unsigned long long)blockIdx.x * kAdvanceThreads + threadIdx.x;
     if (j >= a.rain_count) return;
     const size_t i = (size_t)(a.rain_origin + j);

@@ -6,7 +6,7 @@
  * writes, so the step kernel advances each scatterer and adds it to pulse
  * k + 1 from registers: the state is read and written once per pulse instead
  * of read again by a separate pulse kernel.  The grid is persistent (a few
- * blocks per SM, each looping over the advance's blocks of 256 scatterers)
+ * blocks per SM, each looping over the advance's blocks of kAdvanceThreads scatterers)
  * so that every block's gate bins are added to the FP64 accumulator once.
  * Results are those of the advance kernels followed by k_pulse: the same per-scatterer
  * operations, the gate sums in another order.
