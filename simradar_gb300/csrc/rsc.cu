@@ -560,6 +560,7 @@ void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
     P.rk64 = w->rk64;
     P.G = w->G;
     memcpy(P.sim, sim, sizeof(P.sim));
+    rsc::beam_norm_df(P.sim, P.bn_hi, P.bn_lo);
     P.rs = w->range_start;
     P.inv_delta = w->range_delta != 0.0f ? 1.0f / w->range_delta : 0.0f;
     P.rdelta = w->range_delta;
@@ -2472,6 +2473,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     P.rk = reinterpret_cast<const float *>(b + RSC_NA_RK_OFF);
     P.G = G;
     memcpy(P.sim, sim_desc, sizeof(P.sim));
+    rsc::beam_norm_df(P.sim, P.bn_hi, P.bn_lo);
     P.rs = range_start;
     P.inv_delta = range_delta != 0.0f ? 1.0f / range_delta : 0.0f;
     P.rdelta = range_delta;

@@ -144,6 +144,7 @@ k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *pre
         sp.pulse = out + (size_t)i * out_stride;
         sp.pos = steps[i].pos_r;
         sp.rcs = steps[i].rcs_r;
+        beam_norm_df(steps[i].sim, sp.bn_hi, sp.bn_lo);
     }
     __syncthreads();
     const unsigned b0 = __ldg(prefix + i);

@@ -403,6 +403,7 @@ struct PulseArgs {
     const double *rk64;  /* FP64 (F64 mode) */
     unsigned G;
     float sim[16];
+    float bn_hi, bn_lo;  /* |beam| of sim[0..2] as a double-float (compensated form) */
     float rs, inv_delta, win_lo, win_hi;
     float rdelta;        /* gate spacing: the running sum's increment */
     unsigned rw_n;       /* range weight table length; <= 4 is kept in rwv */
@@ -416,6 +417,15 @@ struct PulseArgs {
     float4 *pulse;
     double *pulse64;
 };
+
+/* The norm of the beam vector sim[0..2] as a double-float, formed once per
+ * pulse in double (the compensated signal divides by |b| |p|). */
+__host__ __device__ inline void beam_norm_df(const float *sim, float &hi, float &lo) {
+    const double x = sim[0], y = sim[1], z = sim[2];
+    const double n = sqrt(x * x + y * y + z * z);
+    hi = (float)n;
+    lo = (float)(n - (double)hi);
+}
 
 /* the pass-1 weight of one gate (rs.cl:1196-1209), bit-exact.  The clamp
  * leaves an integer-valued floor in [0, max] (a NaN index clamps to 0), so

@@ -134,10 +134,7 @@ __device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4
     float c2h, c2l, cnh, cnl;
     df_norm2(ch, cl, c2h, c2l);
     df_sqrt(c2h, c2l, cnh, cnl);
-    const float bh3[3] = {bx, by, bz};
-    float b2h, b2l, bnh, bnl;
-    df_norm2(bh3, pl3, b2h, b2l);
-    df_sqrt(b2h, b2l, bnh, bnl);
+    const float bnh = P.bn_hi, bnl = P.bn_lo;   /* |b|, once per pulse */
     float dph, dpl;                      /* |b| |p| */
     two_prod(bnh, rh, dph, dpl);
     dpl = fmaf(bnh, rl, fmaf(bnl, rh, dpl));
