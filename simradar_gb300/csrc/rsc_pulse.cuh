@@ -79,15 +79,18 @@ __device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, f
     h = s + e;
     l = e - (h - s);
 }
+/* In both the correction c is a few ulps of the head, so an approximate
+ * quotient for it (__fdividef, 2 ulp) leaves the pair accurate to ~1e-14;
+ * the head of the quotient is corrected the same way. */
 __device__ __forceinline__ void df_sqrt(float ah, float al, float &h, float &l) {
     float r = sqrtf(ah);
-    float c = (fmaf(-r, r, ah) + al) / (2.0f * r);
+    float c = __fdividef(fmaf(-r, r, ah) + al, 2.0f * r);
     h = r + c;
     l = c - (h - r);
 }
 __device__ __forceinline__ void df_div(float ah, float al, float bh, float bl, float &h, float &l) {
-    float q = ah / bh;
-    float c = (fmaf(-q, bh, ah) + al - q * bl) / bh;
+    float q = __fdividef(ah, bh);
+    float c = __fdividef(fmaf(-q, bh, ah) + al - q * bl, bh);
     h = q + c;
     l = c - (h - q);
 }
