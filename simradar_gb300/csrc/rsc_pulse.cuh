@@ -103,12 +103,29 @@ __device__ __forceinline__ void df_prod_diff(float a, float b, float c, float d,
 }
 /* sum of squares of three double-floats (the squares of the tails dropped) */
 __device__ __forceinline__ void df_norm2(const float *h3, const float *l3, float &h, float &l) {
-    float sh = 0.0f, sl = 0.0f;
+    float sh, sl;
+    two_prod(h3[0], h3[0], sh, sl);
+    sl = fmaf(2.0f * h3[0], l3[0], sl);
 #pragma unroll
-    for (int i = 0; i < 3; i++) {
+    for (int i = 1; i < 3; i++) {
         float p, pe;
         two_prod(h3[i], h3[i], p, pe);
         pe = fmaf(2.0f * h3[i], l3[i], pe);
+        df_add(sh, sl, p, pe, sh, sl);
+    }
+    h = sh;
+    l = sl;
+}
+
+/* sum of squares of three floats as a double-float (df_norm2 with zero
+ * tails: the first square starts the sum) */
+__device__ __forceinline__ void df_norm2_f(const float *h3, float &h, float &l) {
+    float sh, sl;
+    two_prod(h3[0], h3[0], sh, sl);
+#pragma unroll
+    for (int i = 1; i < 3; i++) {
+        float p, pe;
+        two_prod(h3[i], h3[i], p, pe);
         df_add(sh, sl, p, pe, sh, sl);
     }
     h = sh;
@@ -124,9 +141,9 @@ __device__ __forceinline__ void df_norm2(const float *h3, const float *l3, float
 __device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4 x, Sig32 &o) {
     const float *sd = P.sim;
     /* range */
-    const float ph3[3] = {p.x, p.y, p.z}, pl3[3] = {0.0f, 0.0f, 0.0f};
+    const float ph3[3] = {p.x, p.y, p.z};
     float r2h, r2l, rh, rl;
-    df_norm2(ph3, pl3, r2h, r2l);
+    df_norm2_f(ph3, r2h, r2l);
     df_sqrt(r2h, r2l, rh, rl);
     /* sin of the beam angle */
     const float bx = sd[0], by = sd[1], bz = sd[2];
