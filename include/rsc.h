@@ -304,7 +304,7 @@ int rsc_batch_get_shape(rsc_batch *b, int *warps, int *blocks_per_sm);
  * and the warm-up advance of RS_populate stay in rs.c. */
 typedef struct {
     uint32_t seed;                       /* H->random_seed */
-    uint32_t concept;                    /* H->sim_concept bits */
+    uint32_t sim_concept;                /* H->sim_concept bits */
     float domain_origin[3], domain_size[3];   /* RS_get_domain */
     uint32_t num_types;                  /* H->num_types (1 + debris types) */
     uint64_t origins[RSC_MAX_TYPES], counts[RSC_MAX_TYPES];

@@ -64,7 +64,7 @@ int Generator::init(const rsc_populate_args *args, const char **why) {
         *why = "num_types outside [1, RSC_MAX_TYPES]";
         return RSC_ERR_ARG;
     }
-    if (a.concept & 0x20u) {
+    if (a.sim_concept & 0x20u) {
         *why = "fixed-position scatterers (anchor planes) are populated by rs.c";
         return RSC_ERR_UNSUPPORTED;
     }
@@ -99,7 +99,7 @@ void Generator::fill(size_t n, float *pos4, float *aux4, uint32_t *rnd4, uint32_
         if (next_slot < rain_end && a.dsd_count > 0) {
             const float u = unit(&dsd_rs);
             int bin = 0;
-            if (a.concept & 0x10u) {   /* uniform DSD, scaled RCS */
+            if (a.sim_concept & 0x10u) {   /* uniform DSD, scaled RCS */
                 bin = (int)(u * (float)a.dsd_count);
             } else {
                 for (int k = (int)a.dsd_count - 1; k >= 0; k--) {

@@ -471,7 +471,7 @@ class Batch:
 
 class PopulateArgs(ctypes.Structure):
     """rsc_populate_args: what RS_populate reads from its handle."""
-    _fields_ = [("seed", ctypes.c_uint32), ("concept", ctypes.c_uint32),
+    _fields_ = [("seed", ctypes.c_uint32), ("sim_concept", ctypes.c_uint32),
                 ("domain_origin", ctypes.c_float * 3), ("domain_size", ctypes.c_float * 3),
                 ("num_types", ctypes.c_uint32),
                 ("origins", ctypes.c_uint64 * RSC_MAX_TYPES), ("counts", ctypes.c_uint64 * RSC_MAX_TYPES),
@@ -481,7 +481,7 @@ class PopulateArgs(ctypes.Structure):
     def make(cls, seed, concept, origin, size, counts, dsd_r=None, dsd_cdf=None):
         a = cls()
         a.seed = int(seed) & 0xFFFFFFFF
-        a.concept = int(concept)
+        a.sim_concept = int(concept)
         for k in range(3):
             a.domain_origin[k] = float(origin[k])
             a.domain_size[k] = float(size[k])

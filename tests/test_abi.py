@@ -96,3 +96,18 @@ int main(void) {
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+
+
+@pytest.mark.parametrize("std", ["c++11", "c++17", "c++20"])
+def test_header_compiles_as_cpp(tmp_path, std):
+    """A C++ host (any standard, C++20 keywords included) can include the
+    header as it is."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "host.cpp"
+    src.write_text('#include "rsc.h"\nint main() { rsc_populate_args a = {}; return (int)a.sim_concept; }\n')
+    subprocess.run([gxx, "-std=" + std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                    os.path.join(ROOT, "include"), str(src)], check=True)
