@@ -265,3 +265,46 @@ def test_partial_population_batch_and_worker(backend, oracle_lib):
     assert np.array_equal(bits(st.s["pos"][lo:]), bits(S.state["pos"][lo:]))
     B.close()
     W.close()
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batch_mixed_instances_odd_runs(backend, oracle_lib, use_graph):
+    """A debris-only instance, one whose last debris type lies outside its
+    population and one plain instance, stepped in runs of 1 and 3 steps (each
+    run leaves the state in the other pos / rcs pair): every instance bit-exact
+    against the oracle and its pulses within the summation bound."""
+    O = oracle_lib
+    A = synth.make_scene(num_rain=0, debris=[(synth.OBJ_LEAF, 700), (synth.OBJ_BRICK, 300)], les_count=1, seed=41)
+    push_to_edges(A, n_rain=0, n_deb=40)
+    B = synth.make_scene(num_rain=9000, debris=[(synth.OBJ_LEAF, 200), (synth.OBJ_BRICK, 200)], with_tables=False,
+                         seed=42)
+    C = synth.make_scene(num_rain=4000, with_tables=False, seed=43)
+    for S in (B, C):
+        S.les, S.les_cfg, S.les_desc = A.les, A.les_cfg, A.les_desc
+    scenes = [A, B, C]
+    counts = [list(S.counts) for S in scenes]
+    counts[1][-1] = 0
+    pops = [backend.Population.make(c) for c in counts]
+    ws = []
+    for S in scenes:
+        W = backend.Worker(0)
+        synth.load_worker(W, S)
+        ws.append(W)
+    Bt = backend.Batch(ws)
+    Bt.set_populations(pops)
+    sts = [O.OracleState(S.state) for S in scenes]
+    k0 = 0
+    for run in (1, 3, 1):
+        sims, les = _steps(scenes, k0, run)
+        pulses = Bt.run(sims, les, use_graph=use_graph)
+        for j in range(run):
+            for i, S in enumerate(scenes):
+                direct, ab = O.make_pulse_direct(sts[i], S, sims[j, i], return_abs=True)
+                assert_pulse_close(pulses[j, i, :S.range_count], direct, ab, "instance %d step %d" % (i, k0 + j))
+                O.advance_time(sts[i], S, counts[i], S.les[0], sims[j, i])
+        for i, W in enumerate(ws):
+            assert_state_equal(W.download(STATE_FIELDS), sts[i].s, where="instance %d after step %d " % (i, k0 + run - 1))
+        k0 += run
+    Bt.close()
+    for W in ws:
+        W.close()
