@@ -437,20 +437,26 @@ typedef void (*PulseKernel)(const PulseArgs);
  * the path at run time (one compensated kernel per path measured 7% slower). */
 PulseKernel pulse_kernel(int mode, int path) {
     if (mode == RSC_PULSE_PLAIN) {
+        if (path == 4) return rsc::k_pulse_group<0, kPulseGroup, 1>;
         if (path == 3) return rsc::k_pulse_group<0, kPulseGroup>;
         return path == 2 ? rsc::k_pulse<0, 2> : (path == 1 ? rsc::k_pulse<0, 1> : rsc::k_pulse<0, 0>);
     }
-    if (mode == RSC_PULSE_COMPENSATED) return path == 3 ? rsc::k_pulse_group<1, kPulseGroup> : rsc::k_pulse<1, -1>;
+    if (mode == RSC_PULSE_COMPENSATED) {
+        if (path == 4) return rsc::k_pulse_group<1, kPulseGroup, 1>;
+        return path == 3 ? rsc::k_pulse_group<1, kPulseGroup> : rsc::k_pulse<1, -1>;
+    }
     return rsc::k_pulse<2, -1>;
 }
 
 /* 0 atomics, 1 coherent warps, 2 every gate, 3 coherent warps with
  * kPulseGroup scatterers per lane (the compensated form, and the plain form
- * when it does not write aux / sig) */
+ * when it does not write aux / sig), 4 the same with the triangle range
+ * table compiled in */
 int pulse_path(const PulseArgs &P, int mode) {
     if (P.dense) return 2;
     if (P.coherent_span <= 0) return 0;
-    return ((mode == RSC_PULSE_PLAIN && !P.materialize) || mode == RSC_PULSE_COMPENSATED) ? 3 : 1;
+    if ((mode == RSC_PULSE_PLAIN && !P.materialize) || mode == RSC_PULSE_COMPENSATED) return P.rw_tri ? 4 : 3;
+    return 1;
 }
 
 /* Launch shape of the pulse kernel (one-instance or batched form) for G
@@ -1650,6 +1656,7 @@ struct rsc_batch {
     int mode = RSC_PULSE_PLAIN;
     uint32_t Gmax = 0;
     int tune_warps = 0, tune_per_sm = 0;
+    bool tri = false;   /* the pulse kernel with the triangle range weight compiled in */
     /* per-instance launch descriptors and block prefixes */
     std::vector<rsc::BatchAdvance> h_adv;
     std::vector<PulseArgs> h_pulse;
@@ -1736,6 +1743,7 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
     b->h_rain_prefix.assign(n + 1, 0u);
     b->h_deb_prefix.assign(n + 1, 0u);
     b->h_pulse_prefix.assign(n + 1, 0u);
+    bool tri = true;   /* every instance's range table is the triangle */
     b->concept.assign(n, 0u);
     unsigned acc_r = 0, acc_d = 0, acc_p = 0;
     for (size_t i = 0; i < n; i++) {
@@ -1766,6 +1774,7 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
         fill_pulse_args(x, P, row[i].sim);
         if (b->mode == RSC_PULSE_COMPENSATED) P.rk = x->rk_hi;
         P.materialize = 0;
+        tri = tri && P.rw_tri;
         /* pulse blocks in proportion to the scatterers, at least one, and no
          * block without a scatterer to start on */
         double share = sum_n > 0.0 ? total * (double)x->num_scats / sum_n : 1.0;
@@ -1781,9 +1790,10 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
     b->h_deb_prefix[n] = acc_d;
     b->h_pulse_prefix[n] = acc_p;
     if (acc_r != b->rain_blocks || acc_d != b->deb_blocks || acc_p != b->pulse_blocks || threads != b->pulse_threads ||
-        smem != b->pulse_smem) {
+        smem != b->pulse_smem || tri != b->tri) {
         batch_drop_graph(b);
     }
+    b->tri = tri;
     b->rain_blocks = acc_r;
     b->deb_blocks = acc_d;
     b->pulse_blocks = acc_p;
@@ -1808,8 +1818,12 @@ cudaError_t batch_launch_pulse(rsc_batch *b, int k) {
     float4 *out = b->d_out + (size_t)k * n * b->Gmax;
     const unsigned g = b->pulse_blocks, t = (unsigned)b->pulse_threads;
     const size_t sm = b->pulse_smem;
-    if (b->mode == RSC_PULSE_PLAIN) {
+    if (b->mode == RSC_PULSE_PLAIN && b->tri) {
+        rsc::k_pulse_batch<0, 1><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
+    } else if (b->mode == RSC_PULSE_PLAIN) {
         rsc::k_pulse_batch<0><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
+    } else if (b->mode == RSC_PULSE_COMPENSATED && b->tri) {
+        rsc::k_pulse_batch<1, 1><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
     } else if (b->mode == RSC_PULSE_COMPENSATED) {
         rsc::k_pulse_batch<1><<<g, t, sm, b->stream>>>(b->d_pulse, st, b->d_pulse_prefix, n, out, b->Gmax);
     } else {

@@ -128,7 +128,8 @@ k_advance_batch_debris(const BatchAdvance *inst, const BatchStep *steps, const u
     debris_step(sa, T, (size_t)(T.origin + (j - sa.deb_prefix[t])), pos, rcs, known);
 }
 
-template <int MODE>
+/* TRI 1: every instance's range table is the triangle (compiled in) */
+template <int MODE, int TRI = -1>
 __global__ void __launch_bounds__(512)
 k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *prefix, int ninst, float4 *out,
               unsigned out_stride) {
@@ -151,7 +152,7 @@ k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *pre
     /* an instance whose state is in spatial order takes two scatterers per
      * lane, as the one-instance kernel does */
     if (MODE != 2 && sp.coherent_span > 0 && !sp.materialize) {
-        pulse_body_group<MODE == 2 ? 0 : MODE, 2>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
+        pulse_body_group<MODE == 2 ? 0 : MODE, 2, TRI>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
     } else {
         pulse_body<MODE>(sp, blockIdx.x - b0, __ldg(prefix + i + 1) - b0);
     }

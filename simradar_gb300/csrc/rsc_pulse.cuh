@@ -520,7 +520,7 @@ struct PulseBins {
      * (the same running-sum gate origin from the warp's first gate).  A warp
      * with a non-finite signal takes its scatterers one at a time through
      * add. */
-    template <int K>
+    template <int K, int TRI = -1>   /* TRI 1: the range table is the triangle (known at compile time) */
     __device__ __forceinline__ void add_k(const PulseArgs &P, const bool *in, const unsigned long long *idx,
                                           const float4 *pp, const float4 *xx) {
         static_assert(MODE == 0 || MODE == 1, "the grouped form is the plain or compensated one");
@@ -580,7 +580,9 @@ struct PulseBins {
                 float w = 0.0f;
                 if (gate >= klo[q] && gate <= khi[q]) {
                     if constexpr (MODE == 1) {
-                        w = range_weight_comp(P.rw, P.rwd, P.rw_tri, rr[q] - rk_hi, rl[q] - rk_lo);
+                        w = range_weight_comp(P.rw, P.rwd, TRI == 1 ? 1 : P.rw_tri, rr[q] - rk_hi, rl[q] - rk_lo);
+                    } else if constexpr (TRI == 1) {
+                        w = range_weight_tri(P.rwd, rr[q] - rkj);
                     } else {
                         w = range_weight_reg(P, rr[q] - rkj);
                     }
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
 /* Block blk of the nblk blocks forming one pulse, over a state in spatial
  * order, K scatterers per lane (PulseBins::add_k): warp w of a block takes
  * runs of 32 K neighbours. */
-template <int MODE, int K>
+template <int MODE, int K, int TRI = -1>
 __device__ __forceinline__ void pulse_body_group(const PulseArgs &P, unsigned blk, unsigned nblk) {
     PulseBins<MODE, 1> B;
     B.init(P);
@@ -702,16 +704,17 @@ __device__ __forceinline__ void pulse_body_group(const PulseArgs &P, unsigned bl
                 xx[q] = __ldg(P.rcs + idx[q]);
             }
         }
-        B.template add_k<K>(P, in, idx, pp, xx);
+        B.template add_k<K, TRI>(P, in, idx, pp, xx);
     }
     B.finish(P, nblk);
 }
 
 /* The plain or compensated pulse over a state in spatial order, K
- * scatterers per lane. */
-template <int MODE, int K>
+ * scatterers per lane; TRI 1 when the range table is the triangle (its
+ * closed form compiled in, no table test per gate). */
+template <int MODE, int K, int TRI = -1>
 __global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
-    pulse_body_group<MODE, K>(P, blockIdx.x, gridDim.x);
+    pulse_body_group<MODE, K, TRI>(P, blockIdx.x, gridDim.x);
 }
 
 }  // namespace rsc
