@@ -531,8 +531,13 @@ cudaError_t launch_advance(rsc_worker *w, const AdvanceArgs &a, unsigned blocks,
         (*launched)++;
     }
     if (a.rain_blocks) {
-        if (a.rain_mode == 1) {
+        const bool stretched = rsm_f2u(a.wind[7]) == 7u;   /* the LES index form, fixed per LES */
+        if (a.rain_mode == 1 && stretched) {
+            rsc::k_advance_rain<1, 7><<<a.rain_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
+        } else if (a.rain_mode == 1) {
             rsc::k_advance_rain<1><<<a.rain_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
+        } else if (a.rain_mode == 0 && stretched) {
+            rsc::k_advance_rain<0, 7><<<a.rain_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
         } else if (a.rain_mode == 0) {
             rsc::k_advance_rain<0><<<a.rain_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
         } else {

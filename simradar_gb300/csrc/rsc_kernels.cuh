@@ -55,6 +55,7 @@ struct AdvanceArgs {
 };
 
 /* ---- el_atts (rs.cl:653-739) ---- */
+template <int SP = -1>
 __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const float dt = sd[11];
@@ -84,7 +85,7 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
         xk = false;
         return;
     }
-    float4 bg_vel = compute_bg_vel(pos, a.uvwt, a.wind, sd);
+    float4 bg_vel = compute_bg_vel<SP>(pos, a.uvwt, a.wind, sd);
     float4 dv = f4(bg_vel.x - vel.x, bg_vel.y - vel.y, bg_vel.z - vel.z, bg_vel.w - vel.w);
     float dva = len3(dv.x, dv.y, dv.z);
     const float g_dt = -9.8f * dt;
@@ -119,6 +120,7 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
 }
 
 /* ---- bg_atts (rs.cl:533-580) ---- */
+template <int SP = -1>
 __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
     const float *sd = a.sim;
     const float dt = sd[11];
@@ -142,7 +144,7 @@ __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &
         xk = false;
         return;
     }
-    vel = compute_bg_vel(pos, a.uvwt, a.wind, sd);
+    vel = compute_bg_vel<SP>(pos, a.uvwt, a.wind, sd);
     float4 rcs = compute_ellipsoid_rcs(pos, a.drop, a.drop_desc);
     a.pos[i] = pos;
     a.vel[i] = vel;
@@ -352,7 +354,7 @@ __device__ __forceinline__ bool advance_one(const AdvanceArgs &a, unsigned b, un
  * fill the SM slots the pulse of the same step leaves another 2.3% faster
  * than blocks of 256.  The fused step kernel takes both paths through
  * advance_one. */
-template <int RAIN_MODE>
+template <int RAIN_MODE, int SP = -1>   /* SP: the LES spacing code, when known (7 stretched) */
 __global__ void __launch_bounds__(kAdvanceThreads, 2048 / kAdvanceThreads) k_advance_rain(const AdvanceArgs a) {
     const unsigned long long j = (unsigned long long)blockIdx.x * kAdvanceThreads + threadIdx.x;
     if (j >= a.rain_count) return;
@@ -360,9 +362,9 @@ __global__ void __launch_bounds__(kAdvanceThreads, 2048 / kAdvanceThreads) k_adv
     float4 pos, rcs;
     bool known;
     if (RAIN_MODE == 1) {
-        rain_el(a, i, pos, rcs, known);
+        rain_el<SP>(a, i, pos, rcs, known);
     } else if (RAIN_MODE == 0) {
-        rain_bg(a, i, pos, rcs, known);
+        rain_bg<SP>(a, i, pos, rcs, known);
     } else {
         rain_fp(a, i, pos, rcs, known);
     }

@@ -193,8 +193,10 @@ __device__ __forceinline__ float4 read_image2d(const Image &im, float u, float v
 }
 
 /* wind_table_index (rs.cl:123-188), x/y/z lanes */
+/* SP >= 0: the descriptor's spacing code (wd[7]) known at compile time */
+template <int SP = -1>
 __device__ __forceinline__ void wind_table_index(float out[3], float4 pos, const float *wd, const float *sd) {
-    uint32_t spacing = __float_as_uint(wd[7]);
+    const uint32_t spacing = SP >= 0 ? (uint32_t)SP : __float_as_uint(wd[7]);
     if (spacing == 7u) {
         float pr0 = pos.x - (sd[8] + 0.5f * sd[12]);
         float pr1 = pos.y - (sd[9] + 0.5f * sd[13]);
@@ -211,9 +213,10 @@ __device__ __forceinline__ void wind_table_index(float out[3], float4 pos, const
     }
 }
 
+template <int SP = -1>
 __device__ __forceinline__ float4 compute_bg_vel(float4 pos, const PairImage &uvwt, const float *wd, const float *sd) {
     float c[3];
-    wind_table_index(c, pos, wd, sd);
+    wind_table_index<SP>(c, pos, wd, sd);
     return read_pair_image3d(uvwt, c[0], c[1], c[2]);
 }
 
