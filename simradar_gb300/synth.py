@@ -173,6 +173,172 @@ def write_les_folder(directory, cfg, vols, config="suctvort", volumes_per_file=1
                             marker(4 if last else 4 * nn))
 
 
+# ------------------------------------------- tables identical on every host
+# The files below are made with integer hashing and the correctly rounded
+# IEEE operations (+, -, *, /, sqrt) only -- no libm transcendental -- so the
+# same call writes the same bytes on x86-64 and aarch64.  A session of the
+# reference host recorded on one machine can then be replayed against its
+# tables on another.
+
+_SM_A = np.uint64(0x9E3779B97F4A7C15)
+_SM_B = np.uint64(0xBF58476D1CE4E5B9)
+_SM_C = np.uint64(0x94D049BB133111EB)
+
+
+def hash_uniform(seed, n):
+    """n float32 in [0, 1): splitmix64 of (seed << 32) + i, the top 24 bits
+    times 2^-24 (exact in single precision)."""
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) << np.uint64(32)) + np.arange(n, dtype=np.uint64) + _SM_A
+        z = (z ^ (z >> np.uint64(30))) * _SM_B
+        z = (z ^ (z >> np.uint64(27))) * _SM_C
+        z = z ^ (z >> np.uint64(31))
+    return ((z >> np.uint64(40)).astype(np.float64) * 2.0 ** -24).astype(np.float32)
+
+
+def _powers(r, k):
+    """r ** k for integer k >= 0 by repeated multiplication (float64)."""
+    out = np.ones(len(k), dtype=np.float64)
+    p = 1.0
+    table = [1.0]
+    for _ in range(int(k.max()) if len(k) else 0):
+        p = p * r
+        table.append(p)
+    for i, kk in enumerate(k):
+        out[i] = table[int(kk)]
+    return out
+
+
+def exact_node_km(cfg):
+    """Node coordinates (km) of the stretched grid, texel centres as in
+    LESConfig.node_positions, formed without transcendental functions
+    (half-integer powers as sqrt(r) times integer powers)."""
+    def axis(n, a, r, centred):
+        a, r = float(a), float(r)
+        sr = math.sqrt(r)
+        if centred:
+            # k - c = i + 1 - n / 2 for even n, i + 1/2 - (n - 1) / 2 for odd n
+            d2 = 2 * np.arange(n) + 1 - n          # 2 (k - c), an integer
+            mag = np.abs(d2)
+            whole = _powers(r, mag // 2)
+            pw = np.where(mag % 2 == 1, whole * sr, whole)
+            return np.sign(d2) * (a / (r - 1.0)) * (pw - 1.0)
+        k2 = 2 * np.arange(n) + 1                   # 2 k for k = i + 1/2
+        whole = _powers(r, k2 // 2)
+        pw = np.where(k2 % 2 == 1, whole * sr, whole)
+        return (a / (r - 1.0)) * (pw - 1.0)
+    x = axis(cfg.nx, cfg.ax, cfg.rx, True)
+    y = axis(cfg.ny, cfg.ay, cfg.ry, True)
+    z = axis(cfg.nz, cfg.az, cfg.rz, False)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    return X * 1e-3, Y * 1e-3, Z * 1e-3
+
+
+def exact_les_volumes(cfg=None, count=2, seed=11, vmax=50.0, core=100.0, sigma=3.0):
+    """LES volumes identical on every host: a Scully vortex (tangential speed
+    2 vmax core rho / (rho^2 + core^2), peak vmax at rho = core, a rational
+    function of the node position) with a weak updraft, plus uniform noise of
+    standard deviation sigma from hash_uniform, per volume."""
+    cfg = cfg or LESConfig()
+    X, Y, Z = (a * 1e3 for a in exact_node_km(cfg))
+    rho2 = X * X + Y * Y
+    k = 2.0 * vmax * core / (rho2 + core * core)
+    u0 = -k * Y
+    v0 = k * X
+    w0 = 0.05 * Z * core * core / (rho2 + core * core)
+    p0 = -1.0e3 * core * core / (rho2 + core * core)
+    n = cfg.nx * cfg.ny * cfg.nz
+    amp = sigma * math.sqrt(12.0)
+    vols = []
+    for v in range(count):
+        uvwt = np.zeros((cfg.nz, cfg.ny, cfg.nx, 4), dtype=np.float32)
+        for c, base in enumerate((u0, v0, w0)):
+            noise = (hash_uniform(seed * 1000 + 10 * v + c, n).astype(np.float64) - 0.5) * amp
+            uvwt[..., c] = base + noise.reshape(base.shape)
+        uvwt[..., 3] = (hash_uniform(seed * 1000 + 10 * v + 3, n).astype(np.float64) * 2.0 + 290.0).reshape(u0.shape)
+        cpxx = np.zeros_like(uvwt)
+        cpxx[..., 1] = p0
+        vols.append(LESVolume(uvwt, cpxx))
+    return cfg, vols
+
+
+def write_adm_file(path, cd, cm):
+    """An ADM table file as adm.c reads it (adm.c:168-209): uint16 nb, na,
+    then cdx, cdy, cdz, cmx, cmy, cmz, na x nb floats each (beta fastest).
+    cd, cm: (na, nb, 4) float32 images."""
+    na, nb = cd.shape[:2]
+    with open(path, "wb") as f:
+        f.write(np.array([nb, na], np.uint16).tobytes())
+        for img in (cd, cm):
+            for c in range(3):
+                f.write(np.ascontiguousarray(img[..., c], np.float32).tobytes())
+
+
+def write_rcs_file(path, re, im):
+    """An RCS table file as rcs.c reads it (rcs.c:197-239): uint16 na, nb,
+    then hh, vv, hv real parts and hh, vv, hv imaginary parts, nb x na floats
+    each (alpha fastest).  re, im: (nb, na, 4) float32 images with lanes
+    (hh, vv, hv, 0)."""
+    nb, na = re.shape[:2]
+    with open(path, "wb") as f:
+        f.write(np.array([na, nb], np.uint16).tobytes())
+        for img in (re, im):
+            for c in range(3):
+                f.write(np.ascontiguousarray(img[..., c], np.float32).tobytes())
+
+
+ADM_FILES = ("plate", "square_plate")                    # adm.h: ADMConfig*
+RCS_FILES = ("leaf", "plate", "brick", "woodboard")      # rcs.h: RCSConfig* used by obj.c
+
+
+def exact_adm_images(seed, nb=37, na=19):
+    """(cd, cm) images (na, nb, 4), identical on every host: smooth drag
+    coefficients (a quadratic of the table position) plus hashed noise."""
+    a = np.arange(na, dtype=np.float64)[:, None] / (na - 1)
+    b = np.arange(nb, dtype=np.float64)[None, :] / (nb - 1)
+    cd = np.zeros((na, nb, 4), np.float32)
+    cm = np.zeros((na, nb, 4), np.float32)
+    for c in range(3):
+        h = hash_uniform(seed * 100 + c, na * nb).astype(np.float64).reshape(na, nb)
+        cd[..., c] = (0.6 - (0.5 * c + 1.0) * (a - 0.5) * (b - 0.5)) + 0.2 * (h - 0.5)
+        h = hash_uniform(seed * 100 + 10 + c, na * nb).astype(np.float64).reshape(na, nb)
+        cm[..., c] = 0.2 * (a - 0.5) * (b - 0.5) * (c + 1.0) + 0.05 * (h - 0.5)
+    return cd, cm
+
+
+def exact_rcs_images(seed, na=37, nb=19, level=1.0e-3):
+    """(real, imag) images (nb, na, 4) with lanes (hh, vv, hv, 0), identical
+    on every host: hashed values of magnitude ~level (hv a fifth of it)."""
+    re = np.zeros((nb, na, 4), np.float32)
+    im = np.zeros((nb, na, 4), np.float32)
+    for c in range(3):
+        s = 0.2 if c == 2 else 1.0
+        re[..., c] = (level * s * (hash_uniform(seed * 100 + c, na * nb).astype(np.float64) * 2.0 - 1.0)).reshape(nb, na)
+        im[..., c] = (level * s * (hash_uniform(seed * 100 + 10 + c, na * nb).astype(np.float64) * 2.0 - 1.0)).reshape(nb, na)
+    return re, im
+
+
+def write_tables_folder(root, les_cfg=None, les_vols=None, les_config="suctvort", volumes_per_file=10,
+                        adm_dims=(37, 19), rcs_dims=(37, 19), seed=7):
+    """The reference's tables folder (what it finds at ~/Documents/tables,
+    les.c:71-126, adm.c:56-110, rcs.c:93-145): les/<config>/ with the grid and
+    frame files, adm/<name>.adm and rcs/<name>.rcs for every table obj.c
+    names.  All content is identical on every host (exact_* generators)."""
+    if les_vols is None:
+        les_cfg, les_vols = exact_les_volumes(les_cfg, count=2, seed=seed)
+    write_les_folder(os.path.join(root, "les", les_config), les_cfg, les_vols, config=les_config,
+                     volumes_per_file=volumes_per_file, node_km=exact_node_km(les_cfg))
+    os.makedirs(os.path.join(root, "adm"), exist_ok=True)
+    os.makedirs(os.path.join(root, "rcs"), exist_ok=True)
+    for t, name in enumerate(ADM_FILES):
+        cd, cm = exact_adm_images(seed + 10 + t, *adm_dims)
+        write_adm_file(os.path.join(root, "adm", name + ".adm"), cd, cm)
+    for t, name in enumerate(RCS_FILES):
+        re, im = exact_rcs_images(seed + 20 + t, *rcs_dims)
+        write_rcs_file(os.path.join(root, "rcs", name + ".rcs"), re, im)
+    return les_cfg, les_vols
+
+
 # ---------------------------------------------------------------- debris tables
 OBJ_LEAF, OBJ_WOODBOARD_2X4, OBJ_BRICK = 1, 3, 6
 # dimensions (m) and density (kg m^-3) per object (obj.c:102-148)
