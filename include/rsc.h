@@ -127,8 +127,10 @@ int rsc_upload(rsc_worker *w, size_t offset, size_t count, const float *pos4, co
 
 /* Device -> host copy, same convention -- RS_download (rs.c:4961-5016),
  * RS_download_position_only (rs.c:5018-5040), RS_download_orientation_only
- * (rs.c:5042-5064).  aux and sig are formed for the latest pulse first if the
- * pulse kernel did not write them. */
+ * (rs.c:5042-5064).  aux and sig are those of the latest pulse, as rs.c's
+ * last scat_sig_aux launch leaves them: when the pulse kernel did not write
+ * them, they are formed from the state that pulse read (before a second
+ * advance, a sort or an upload replaces it, or here). */
 int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float *vel4, float *ori4,
                  float *tum4, float *aux4, float *rcs4, float *sig4, uint32_t *rnd4);
 
@@ -423,30 +425,33 @@ const char *rsc_les_last_error(void);
 
 /* Form a pulse without allocating any device memory.  This entry point has no
  * counterpart in the reference: it is for callers that cannot call cudaMalloc
- * -- a real-time pulse loop that must not allocate, an application whose
- * device memory is owned by another allocator or already fully reserved, or
- * code whose allocation calls are forbidden while it records work -- and that
- * already hold the scatterer arrays in their own device buffers.
+ * -- a real-time pulse loop that must not allocate, or an application whose
+ * device memory is owned by another allocator or already fully reserved --
+ * and that already hold the scatterer arrays in their own device buffers.
  *
  * Inputs: pos4 and rcs4 are device arrays of num_scats float4; pulse4 is a
  * device array of range_count float4 that receives the per-gate (Ih, Qh, Iv,
  * Qv) sums (no gain applied).  The weight tables, their descriptors and
- * sim_desc are host arrays, copied before the launch.  The pulse is the one
- * rsc_make_pulse forms in RSC_PULSE_PLAIN mode.  Work is queued on `stream`
- * (a cudaStream_t, NULL for the default stream); the call does not wait.
+ * sim_desc are host arrays read during the call: they travel to the device
+ * by value in the launch parameters of two kernels (a one-block set-up that
+ * fills the scratch, then the pulse), so the call queues no host-to-device
+ * copy, reads no host memory after it returns, and does not wait for earlier
+ * work on `stream` (a cudaStream_t, NULL for the default stream).  The pulse
+ * is the one rsc_make_pulse forms in RSC_PULSE_PLAIN mode.
  *
- * The scratch the kernel needs (an FP64 accumulator per gate, a completion
+ * The scratch the kernels need (an FP64 accumulator per gate, a completion
  * counter, gate origins, the weight tables) lives in one fixed __device__
  * array in the library instead of in memory the call allocates: every GPU
  * that loads the library holds about 9 KB for it until the process exits.
  * The accumulator and the counter are cleared at each call.  The first call
  * on a device looks the array's address up (once per device, with that
- * device current); make that first call before any stream capture.  All calls
- * share the one array and it keeps the contents of the last call: two calls
- * whose work overlaps on the GPU race, so
- * order them on one stream or synchronise between them.  Sizes above the
- * RSC_NOALLOC_* limits return RSC_ERR_ARG with a message naming the limit.
- * No cudaMalloc, cudaFree or other allocating call is made. */
+ * device current); make that first call before any stream capture.  All
+ * calls share the one array and it keeps the contents of the last call: two
+ * calls whose work overlaps on the GPU race, so order them on one stream or
+ * synchronise between them.  Sizes above the RSC_NOALLOC_* limits, and a
+ * descriptor whose max index is not inside its table, return RSC_ERR_ARG with
+ * a message naming the limit.  No cudaMalloc, cudaFree or other allocating
+ * call is made. */
 int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scats, const float *range_weight,
                            uint32_t range_n, const float range_desc[4], const float *angular_weight,
                            uint32_t angular_n, const float angular_desc[4], float range_start, float range_delta,

@@ -161,6 +161,26 @@ def read_session(path):
     return out
 
 
+_CODE = {np.dtype(np.float32): "f4", np.dtype(np.uint32): "u4", np.dtype(np.int32): "i4",
+         np.dtype(np.float64): "f8", np.dtype(np.uint64): "u8"}
+
+
+def write_session(path, arrays):
+    """Write named arrays as a record file (the format read_session reads and
+    tests/c/host_loop.c takes); entries of other types are left out."""
+    with open(path, "wb") as f:
+        f.write(b"RSREF001")
+        for name, v in arrays.items():
+            a = np.asarray(v)
+            if a.dtype not in _CODE:
+                continue
+            a = np.ascontiguousarray(a)
+            shape = list(a.shape) + [0] * (4 - a.ndim)
+            f.write(name.encode().ljust(48, b"\0") + _CODE[a.dtype].encode().ljust(8, b"\0"))
+            f.write(np.array([a.ndim, 0], np.uint32).tobytes() + np.array(shape, np.uint64).tobytes())
+            f.write(np.array([a.nbytes], np.uint64).tobytes() + a.tobytes())
+
+
 def run_session(out_path, home, density=0.3, pulses=20, warmup=130, debris=(), seed=19760520, gate=30.0,
                 scan="P:3.0,-12:12:0.24", concept=None, les="suctvort", threads=None):
     """Run refdrive (rs.c on the oracle device) with the tables under

@@ -123,6 +123,9 @@ struct rsc_worker {
     int materialize = 0;
     bool sig_aux_stale = false;
     bool have_pulse_desc = false;
+    /* the pos / rcs pair the latest pulse read: its aux / sig, when the pulse
+     * kernel did not write them, are formed from this pair */
+    const float4 *sa_pos = nullptr, *sa_rcs = nullptr;
     float last_sim[16] = {0};
     uint64_t launches = 0;
     /* pulse launch shape chosen by rsc_autotune (0: default) */
@@ -1112,12 +1115,36 @@ static int sort_worker(rsc_worker *w, const rsc_population *pop, const float *si
     return RSC_OK;
 }
 
+/* aux / sig of the latest pulse (scat_sig_aux, rs.cl:1050-1110) when the
+ * pulse kernel did not write them: formed on `st` from the pos / rcs pair
+ * that pulse read and its descriptor.  rs.c's RS_download returns what the
+ * last scat_sig_aux launch wrote, so they are formed before anything
+ * overwrites or reorders that pair (a second advance, a sort, an upload, a
+ * batch run), or on download. */
+static int settle_sig_aux(rsc_worker *w, cudaStream_t st) {
+    if (!w->sig_aux_stale || !w->have_pulse_desc) return RSC_OK;
+    PulseArgs P;
+    fill_pulse_args(w, P, w->last_sim);
+    if (w->sa_pos != nullptr) {
+        P.pos = w->sa_pos;
+        P.rcs = w->sa_rcs;
+    }
+    const unsigned blocks = (unsigned)((w->num_scats + 255) / 256);
+    rsc::k_sig_aux<<<blocks, 256, 0, st>>>(P);
+    RSC_CUDA(cudaGetLastError());
+    w->launches++;
+    w->sig_aux_stale = false;
+    return RSC_OK;
+}
+
 /* Sort when the interval has passed or the state was replaced. */
 static int maybe_sort(rsc_worker *w, const rsc_population *pop, const float *sim, cudaStream_t st) {
     if (w->sort_interval <= 0) return RSC_OK;
     if (!w->sort_due && w->since_sort < (uint64_t)w->sort_interval) return RSC_OK;
     /* the arrays move: after the advance stream, before its next advance */
     int s = join_adv(w);
+    if (s) return s;
+    s = settle_sig_aux(w, st);
     if (s) return s;
     s = sort_worker(w, pop, sim, st);
     if (s) return s;
@@ -1265,6 +1292,8 @@ int rsc_upload(rsc_worker *w, size_t offset, size_t count, const float *pos4, co
     if (s) return s;
     s = flush_pending(w);
     if (s) return s;
+    s = settle_sig_aux(w, w->stream);
+    if (s) return s;
     if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "upload [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
     const size_t b = count * 16;
     uint4 **arr[8];
@@ -1310,14 +1339,9 @@ int rsc_download(rsc_worker *w, size_t offset, size_t count, float *pos4, float 
     s = flush_pending(w);
     if (s) return s;
     if (offset + count > w->num_scats) return fail(RSC_ERR_ARG, "download [%zu, %zu) beyond %zu", offset, offset + count, w->num_scats);
-    if ((aux4 || sig4) && w->sig_aux_stale && w->have_pulse_desc) {
-        PulseArgs P;
-        fill_pulse_args(w, P, w->last_sim);
-        unsigned blocks = (unsigned)((w->num_scats + 255) / 256);
-        rsc::k_sig_aux<<<blocks, 256, 0, w->stream>>>(P);
-        RSC_CUDA(cudaGetLastError());
-        w->launches++;
-        w->sig_aux_stale = false;
+    if (aux4 || sig4) {
+        s = settle_sig_aux(w, w->stream);
+        if (s) return s;
     }
     const size_t b = count * 16;
     uint4 **arr[8];
@@ -1424,6 +1448,8 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
          * in place on the worker's stream */
         s = les_slot_wait(w, les_id, w->stream);
         if (s) return s;
+        s = settle_sig_aux(w, w->stream);   /* the recorded advance runs in place */
+        if (s) return s;
         w->pend = true;
         w->pend_a = a;
         w->pend_blocks = blocks;
@@ -1448,6 +1474,11 @@ int rsc_advance_time(rsc_worker *w, const rsc_population *pop, int les_id, const
     }
     s = les_slot_wait(w, les_id, w->adv);
     if (s) return s;
+    if (w->sig_aux_stale && w->sa_pos == w->pos_next) {
+        /* a second advance since the pulse overwrites the pair it read */
+        s = settle_sig_aux(w, w->adv);
+        if (s) return s;
+    }
     s = copy_unadvanced(w, pop, w->adv);
     if (s) return s;
     int n = 0;
@@ -1526,6 +1557,8 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
         memcpy(w->last_sim, sim_desc, sizeof(w->last_sim));
         w->have_pulse_desc = true;
         w->sig_aux_stale = !mat;
+        w->sa_pos = w->pos;
+        w->sa_rcs = w->rcs;
         w->since_sort++;
         return maybe_sort(w, &w->pend_pop, w->pend_sim, w->stream);
     }
@@ -1539,6 +1572,8 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     memcpy(w->last_sim, sim_desc, sizeof(w->last_sim));
     w->have_pulse_desc = true;
     w->sig_aux_stale = !mat;
+    w->sa_pos = P.pos;
+    w->sa_rcs = P.rcs;
     return RSC_OK;
 }
 
@@ -2241,6 +2276,11 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
     if (s) return s;
     s = batch_fill_steps(b, steps, sim_descs, les_ids);
     if (s) return s;
+    for (rsc_worker *x : b->w) {
+        s = flush_pending(x);
+        if (s == RSC_OK) s = settle_sig_aux(x, x->stream);
+        if (s) return s;
+    }
     s = batch_join_workers(b);
     if (s) return s;
     const size_t n = b->w.size();
@@ -2301,6 +2341,10 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
         memcpy(x->last_sim, sim_descs + ((size_t)(steps - 1) * n + i) * 16, sizeof(x->last_sim));
         x->have_pulse_desc = true;
         x->sig_aux_stale = true;
+        /* the last step's pulse read the pair its advance did not write */
+        const bool advanced = b->rain_blocks != 0 || b->deb_blocks != 0;
+        x->sa_pos = advanced ? x->pos_next : x->pos;
+        x->sa_rcs = advanced ? x->rcs_next : x->rcs;
     }
     if (pulses_out && wait) RSC_CUDA(cudaStreamSynchronize(b->stream));
     return RSC_OK;
@@ -2431,6 +2475,39 @@ int noalloc_scratch(void **out) {
     return RSC_OK;
 }
 
+/* What the pulse kernel's scratch must hold before it runs, passed by value
+ * in the launch's parameters (about 4.4 KB), so the call reads no host
+ * memory after it returns and queues no host-to-device copy. */
+struct NoAllocSetup {
+    float rw[RSC_NOALLOC_MAX_RANGE_TABLE];
+    float aw[RSC_NOALLOC_MAX_ANGULAR_TABLE];
+    uint32_t rw_n, aw_n, G;
+    float range_start, range_delta;
+    unsigned char *scratch;
+};
+
+/* Fill the scratch: the weight tables, the gate origins as the FP32 running
+ * sum of make_pulse_pass_1 (rs.cl:1214), and a zero accumulator and counter
+ * (the pulse kernel leaves both at zero, but a launch that failed part way
+ * might not have).  One block. */
+__global__ void __launch_bounds__(256) k_noalloc_setup(const NoAllocSetup a) {
+    float *rk = reinterpret_cast<float *>(a.scratch + RSC_NA_RK_OFF);
+    float *rw = reinterpret_cast<float *>(a.scratch + RSC_NA_RW_OFF);
+    float *aw = reinterpret_cast<float *>(a.scratch + RSC_NA_AW_OFF);
+    double *acc = reinterpret_cast<double *>(a.scratch + RSC_NA_ACC_OFF);
+    for (uint32_t i = threadIdx.x; i < a.rw_n; i += blockDim.x) rw[i] = a.rw[i];
+    for (uint32_t i = threadIdx.x; i < a.aw_n; i += blockDim.x) aw[i] = a.aw[i];
+    for (uint32_t i = threadIdx.x; i < 4 * a.G; i += blockDim.x) acc[i] = 0.0;
+    if (threadIdx.x == 0) {
+        float r = a.range_start;
+        for (uint32_t k = 0; k < a.G; k++) {
+            rk[k] = r;
+            r = r + a.range_delta;
+        }
+        *reinterpret_cast<unsigned *>(a.scratch + RSC_NA_COUNTER_OFF) = 0u;
+    }
+}
+
 }  // namespace
 
 int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scats, const float *range_weight,
@@ -2454,8 +2531,10 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
         return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: angular weight table of %u entries, limit %d", angular_n,
                     RSC_NOALLOC_MAX_ANGULAR_TABLE);
     }
-    if (!(range_desc[2] >= 0.0f) || (uint32_t)range_desc[2] >= range_n || !(angular_desc[2] >= 0.0f) ||
-        (uint32_t)angular_desc[2] >= angular_n) {
+    /* the descriptors' max index must lie inside the table: compared as
+     * floats before any conversion (a NaN or a huge value fails here) */
+    if (!(range_desc[2] >= 0.0f && range_desc[2] < (float)range_n) ||
+        !(angular_desc[2] >= 0.0f && angular_desc[2] < (float)angular_n)) {
         return fail(RSC_ERR_ARG, "rsc_make_pulse_noalloc: table max index beyond its table");
     }
     if (!(fabsf(range_start) < INFINITY) || !(fabsf(range_delta) < INFINITY)) {
@@ -2467,19 +2546,16 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     unsigned char *b = static_cast<unsigned char *>(base);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint32_t G = range_count;
-    /* gate origins: the FP32 running sum of make_pulse_pass_1 (rs.cl:1214) */
-    float rk[RSC_NOALLOC_MAX_GATES];
-    float r = range_start;
-    for (uint32_t k = 0; k < G; k++) {
-        rk[k] = r;
-        r = r + range_delta;
-    }
-    RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_RK_OFF, rk, G * sizeof(float), cudaMemcpyHostToDevice, st));
-    RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_RW_OFF, range_weight, range_n * sizeof(float), cudaMemcpyHostToDevice, st));
-    RSC_CUDA(cudaMemcpyAsync(b + RSC_NA_AW_OFF, angular_weight, angular_n * sizeof(float), cudaMemcpyHostToDevice, st));
-    /* the accumulator and the counter must start at zero */
-    RSC_CUDA(cudaMemsetAsync(b + RSC_NA_ACC_OFF, 0, (size_t)G * 4 * sizeof(double), st));
-    RSC_CUDA(cudaMemsetAsync(b + RSC_NA_COUNTER_OFF, 0, sizeof(unsigned), st));
+    NoAllocSetup setup;
+    memset(&setup, 0, sizeof(setup));
+    memcpy(setup.rw, range_weight, range_n * sizeof(float));
+    memcpy(setup.aw, angular_weight, angular_n * sizeof(float));
+    setup.rw_n = range_n;
+    setup.aw_n = angular_n;
+    setup.G = G;
+    setup.range_start = range_start;
+    setup.range_delta = range_delta;
+    setup.scratch = b;
     PulseArgs P;
     memset(&P, 0, sizeof(P));
     P.pos = reinterpret_cast<const float4 *>(pos4);
@@ -2502,14 +2578,17 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     P.acc64 = reinterpret_cast<double *>(b + RSC_NA_ACC_OFF);
     P.counter = reinterpret_cast<unsigned *>(b + RSC_NA_COUNTER_OFF);
     P.pulse = reinterpret_cast<float4 *>(pulse4);
-    /* sparse gate window when both edge weights are zero (see fill_pulse_args) */
+    /* sparse gate window when both edge weights are zero (see fill_pulse_args);
+     * the drift of the FP32 running sum is measured on the host */
     P.dense = 1;
     const float xs = range_desc[0], x0 = range_desc[1], xm = range_desc[2];
     if (range_delta > 0.0f && xs > 0.0f && range_weight[0] == 0.0f && range_weight[(uint32_t)xm] == 0.0f) {
         double d_lo = -(double)x0 / (double)xs, d_hi = ((double)xm - (double)x0) / (double)xs;
         double drift = 0.0;
+        float rf = range_start;
         for (uint32_t k = 0; k < G; k++) {
-            drift = fmax(drift, fabs((double)rk[k] - ((double)range_start + (double)k * (double)range_delta)));
+            drift = fmax(drift, fabs((double)rf - ((double)range_start + (double)k * (double)range_delta)));
+            rf = rf + range_delta;
         }
         double margin = (drift + 1.0e-3 * fabs((double)range_delta)) / (double)range_delta + 0.05;
         double lo = d_lo / (double)range_delta - margin, hi = d_hi / (double)range_delta + margin;
@@ -2519,7 +2598,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
             P.win_hi = (float)hi;
         }
     }
-    /* launch geometry of the plain pulse kernel, capped to the scratch size */
+    /* launch geometry of the plain pulse kernel */
     const PulseKernel kern = pulse_kernel(RSC_PULSE_PLAIN, pulse_path(P, RSC_PULSE_PLAIN));
     int dev = 0, sms = 0, per_sm = 1;
     RSC_CUDA(cudaGetDevice(&dev));
@@ -2530,6 +2609,8 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
     if (per_sm < 1) per_sm = 1;
     if (per_sm > 4) per_sm = 4;
     const int grid = sms * per_sm;
+    k_noalloc_setup<<<1, 256, 0, st>>>(setup);
+    RSC_CUDA(cudaGetLastError());
     kern<<<grid, threads, smem, st>>>(P);
     RSC_CUDA(cudaGetLastError());
     return RSC_OK;
