@@ -60,6 +60,7 @@ GATES = 40
 METRIC = "pulses/s and scatterer-updates/s at 2M scatterers; HBM roofline frac; I/Q err vs FP64"
 UNIT = "pulses/s"
 SECTIONS = ("precision", "batch", "les", "large")
+SORT_INTERVAL = 128   # the backend's default (rsc_set_sort_interval)
 
 
 def workload_config(n_rain):
@@ -305,10 +306,12 @@ def iq_errors(got, ref):
     return {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt((rel ** 2).mean())),
             "p99_rel": float(np.percentile(rel, 99)), "max_rel_raw": float(raw.max()),
             "within_1e-5": float((rel <= 1.0e-5).mean()), "eps": "%g x RMS gate magnitude" % EPS_REL,
-            "values": int(rel.size)}
+            "values": int(rel.size), "above_1e-5": int((rel > 1.0e-5).sum()),
+            "p999_rel": float(np.percentile(rel, 99.9)),
+            "abs_err_over_rms_max": float(e.max() / max(float(np.sqrt((m ** 2).mean())), 1e-300))}
 
 
-def bench_precision(torch, rsc, synth, dev, steps):
+def bench_precision(torch, rsc, synth, dev, steps, n_err=2000):
     n = 8388608
     S = synth.make_scene(num_rain=n, gates=GATES, les_count=1, range_offset=30000.0, seed=4242,
                          scan=synth.ppi_positions(0.7, -0.6, 0.6, 0.012))
@@ -317,8 +320,8 @@ def bench_precision(torch, rsc, synth, dev, steps):
     W = rsc.Worker(dev)
     synth.load_worker(W, S)
     S.state = None
-    n_err = 64
     got = {m: np.zeros((n_err, GATES, 4), np.float32) for m in (0, 1, 2)}
+    t_err = time.perf_counter()
     for k in range(n_err):
         sd = sd_seq[k % len(sd_seq)]
         for m in (2, 1, 0):
@@ -326,6 +329,7 @@ def bench_precision(torch, rsc, synth, dev, steps):
             W.make_pulse(sd)
             W.download_pulse(1.0, out=got[m][k])
         W.advance_time(pop, 0, sd)
+    t_err = time.perf_counter() - t_err
     z64, r64, ok = gate_stats(got[2])
     out = {"workload": "8,388,608 rain, box and 40 gates 30 km out (gates from 31,850 m), PPI 0.7 deg "
                        "-0.6..0.6 deg / 0.012 deg, concept DBU; errors over %d pulses against the FP64 pulse "
@@ -347,6 +351,8 @@ def bench_precision(torch, rsc, synth, dev, steps):
                         "pulse_ms": statistics.mean(tp), "advance_ms": statistics.mean(ta)}
     out["throughput"] = timing
     out["timed_steps"] = steps
+    out["error_pulses"] = n_err
+    out["error_run_s"] = t_err
     W.close()
     return out
 
@@ -406,30 +412,39 @@ def bench_batch(torch, rsc, synth, dev, steps):
             W.advance_time(p, 0, sd)
     torch.cuda.synchronize()
     seqs = [[synth.pulse_sim_desc(S, k, tic=k * 1e-3) for k in range(steps)] for S in scenes]
-    t0 = time.perf_counter()
-    for W, seq, p in zip(ws, seqs, pops):
-        for k in range(steps):
-            W.make_pulse(seq[k])
-            W.download_pulse(1.0, out=hp)
-            W.advance_time(p, 0, seq[k])
-        W.synchronize()
-    wall_b2b = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    for W, seq, p in zip(ws, seqs, pops):
-        for k in range(steps):
-            W.make_pulse(seq[k])
-            W.advance_time(p, 0, seq[k])
-        W.synchronize()
-    wall_b2b_nodl = time.perf_counter() - t0
+    ring = torch.empty((steps, GATES, 4), dtype=torch.float32).pin_memory().numpy()
+
+    def back_to_back(copy):
+        t0 = time.perf_counter()
+        for W, seq, p in zip(ws, seqs, pops):
+            for k in range(steps):
+                W.make_pulse(seq[k])
+                if copy == "async":
+                    W.download_pulse_async(ring[k])
+                elif copy == "blocking":
+                    W.download_pulse(1.0, out=hp)
+                W.advance_time(p, 0, seq[k])
+            W.synchronize()
+        return time.perf_counter() - t0
+
+    wall_async = back_to_back("async")
+    wall_blocking = back_to_back("blocking")
+    wall_none = back_to_back("none")
     for W in ws:
         W.close()
-    res["back_to_back"] = {"pulses_per_s": count * steps / wall_b2b,
-                           "pulses_per_s_no_download": count * steps / wall_b2b_nodl}
-    res["speedup_vs_back_to_back"] = res["batched_graph"]["pulses_per_s"] / res["back_to_back"]["pulses_per_s"]
+    res["back_to_back"] = {"pulses_per_s": count * steps / wall_async,
+                           "pulses_per_s_blocking_read": count * steps / wall_blocking,
+                           "pulses_per_s_no_download": count * steps / wall_none}
+    bg = res["batched_graph"]["pulses_per_s"]
+    res["speedup_vs_back_to_back"] = bg / res["back_to_back"]["pulses_per_s"]
+    res["speedup_vs_back_to_back_blocking_read"] = bg / res["back_to_back"]["pulses_per_s_blocking_read"]
+    res["speedup_vs_back_to_back_no_download"] = bg / res["back_to_back"]["pulses_per_s_no_download"]
     res["workload"] = ("64 instances, scatterers log-uniform 65,536-4,194,304 (total %d), debris 0-4096 per type, "
                        "Marshall-Palmer N0 4000-16000, PPI / RHI alternating, %d gates, compensated form; %d steps "
-                       "timed per instance, pulses copied to the host (batched: once per run; back to back: per "
-                       "pulse)" % (total, GATES, steps))
+                       "timed per instance.  Every pulse reaches the host in both: batched, one copy per run; back "
+                       "to back, each pulse copied to page-locked memory in stream order with one wait per "
+                       "instance (speedup_vs_back_to_back).  Secondary: back to back with a blocking read of every "
+                       "pulse as rs.c does, and with no pulse copied" % (total, GATES, steps))
     res["pulse_shape"] = {"warps": shape[0], "blocks_per_sm": shape[1]}
     res["scatterer_updates_per_s"] = res["batched_graph"]["pulses_per_s"] / count * total
     return res
@@ -452,10 +467,14 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     W.set_precision(rsc.PULSE_COMPENSATED)
     nscat = S.num_scats
     S.state = None
-    # the next LES frame in page-locked memory, for the refill of slot 1
+    # the LES frames in page-locked memory for the refills: frame f of the
+    # run is the synthetic volume f % 2 (two volumes of the recipe alternate)
     nxt = S.les[1]
-    pin_u = torch.from_numpy(np.ascontiguousarray(nxt.uvwt)).pin_memory()
-    pin_c = torch.from_numpy(np.ascontiguousarray(nxt.cpxx)).pin_memory()
+    pinned = [(torch.from_numpy(np.ascontiguousarray(v.uvwt)).pin_memory(),
+               torch.from_numpy(np.ascontiguousarray(v.cpxx)).pin_memory()) for v in S.les[:2]]
+    tp = float(S.les_cfg.tp)
+    # chunk c forms pulses chunk (c + 1) ... (the first chunk is the warm-up run)
+    frame_of = [int(math.floor((c + 1) * chunk * float(S.prt) / tp + 1e-9)) for c in range(chunks + 1)]
     B = rsc.Batch([W])
     B.set_populations([pop])
     B.set_precision(rsc.PULSE_COMPENSATED)
@@ -493,7 +512,7 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    swap_at = chunks // 2
+    swaps = 0
 
     def drain(r):
         ev, c = done[r]
@@ -506,14 +525,19 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
         r = c % 2
         if done[r] is not None:
             drain(r)
-        slot = 1 if c >= swap_at else 0
+        # the frame of this chunk's simulation time (a new one every tp, as
+        # RS_advance_time swaps, rs.c:5188-5200) in slot frame % 2
+        slot = frame_of[c] % 2
         B.run(sims(chunk * (c + 1)), les_ids(slot), out=ring[r].numpy(), wait=False)
         ev = torch.cuda.Event()
         ev.record(stream)
         done[r] = (ev, c)
-        if c == swap_at - 1:
-            # refill slot 1 while this chunk runs on slot 0
-            B.set_les_async(0, 1, pin_u.numpy(), pin_c.numpy())
+        if frame_of[c + 1] != frame_of[c] and c + 1 < chunks:
+            # the next frame into the other slot while this chunk runs
+            f = frame_of[c + 1]
+            u, cp = pinned[f % 2]
+            B.set_les_async(0, f % 2, u.numpy(), cp.numpy())
+            swaps += 1
     e1.record(stream)
     for r in (chunks % 2, (chunks + 1) % 2):
         if done[r] is not None:
@@ -536,10 +560,13 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
     W.close()
     iq = d["iq"]
     return {"workload": "33,554,432 rain + 131,072 debris (leaf / 2x4 board / brick), LES 352x352x160, RHI 0.5-20 "
-                        "deg / 0.02 deg, %d gates, compensated form; %d pulses in chunks of %d streamed to pinned "
-                        "host buffers and on to a .iq file (background writer), LES slot 1 refilled (2 x %d MB) on "
-                        "the copy stream during chunk %d" % (GATES, pulses, chunk, int(nxt.uvwt.nbytes / 1e6),
-                                                               swap_at - 1),
+                        "deg / 0.02 deg (976 positions, repeated), %d gates, compensated form; %d pulses at PRT 1 ms "
+                        "in chunks of %d streamed to pinned host buffers and on to a .iq file (background writer); "
+                        "a new LES frame every tp = %g s of simulation time (les.c:170), %d swaps, each frame "
+                        "(2 x %d MB, two synthetic volumes alternating) refilled on the copy stream into the "
+                        "inactive slot during the chunk before it is used" % (
+                            GATES, pulses, chunk, tp, swaps, int(nxt.uvwt.nbytes / 1e6)),
+            "les_swaps": swaps,
             "pulses_per_s": pulses / wall, "device_pulses_per_s": pulses / (dev_ms / 1e3),
             "scatterer_updates_per_s": pulses / wall * nscat, "pulses": pulses,
             "populate_s": populate_s,
@@ -639,8 +666,19 @@ def run_ours(args, rank, world):
         W.advance_time(pop, 0, sd_seq[k % len(sd_seq)])
     W.synchronize()
 
+    # the periodic spatial sort (every `interval` advances): its cost per sort,
+    # from steps that each sort (interval 1) against steps that do not
+    interval = SORT_INTERVAL
+    W.set_sort_interval(1)
+    ts_sort, _, _ = timed_steps(torch, W, pop, sd_seq, 8, flush=flush)
+    W.set_sort_interval(0)
+    ts_plain, _, _ = timed_steps(torch, W, pop, sd_seq, 8, flush=flush)
+    W.set_sort_interval(interval)
+    sort_ms = max(0.0, statistics.median(ts_sort) - statistics.median(ts_plain))
+
     # device-timed value: per-step events, L2 flushed between steps
     launches0 = W.launch_count
+    sorts0 = W.sort_count
     clocks = ClockSampler(dev)
     clocks.start()
     if world > 1:
@@ -649,7 +687,10 @@ def run_ours(args, rank, world):
     if world > 1:
         torch.distributed.barrier()
     launches = W.launch_count - launches0
-    total_ms = sum(t_step)
+    sorts_value = W.sort_count - sorts0
+    # value carries the sort's amortised cost whatever the window holds: the
+    # sorts that fell in it are taken out and steps / interval of them put in
+    total_ms = sum(t_step) + (args.steps / interval - sorts_value) * sort_ms
 
     # e2e through the C ABI with host buffers: every step's pulse is copied to
     # page-locked host memory in stream order (the host queues the next steps
@@ -657,6 +698,7 @@ def run_ours(args, rank, world):
     ring = torch.empty((args.steps, G, 4), dtype=torch.float32).pin_memory()
     ring_np = ring.numpy()
     W.synchronize()
+    sorts0 = W.sort_count
     t0 = time.perf_counter()
     for k in range(args.steps):
         sd = sd_seq[k % len(sd_seq)]
@@ -666,9 +708,12 @@ def run_ours(args, rank, world):
     W.synchronize()
     ring_np *= np.float32(gain)
     e2e_ms = (time.perf_counter() - t0) * 1000.0
+    sorts_e2e = W.sort_count - sorts0
+    e2e_ms += (args.steps / interval - sorts_e2e) * sort_ms
     # the same with a blocking read of every pulse before the next step, as
     # rs.c reads them (clEnqueueReadBuffer + wait per pulse)
     W.synchronize()
+    sorts0 = W.sort_count
     t0 = time.perf_counter()
     for k in range(args.steps):
         sd = sd_seq[k % len(sd_seq)]
@@ -677,6 +722,7 @@ def run_ours(args, rank, world):
         W.advance_time(pop, 0, sd)
     W.synchronize()
     e2e_blocking_ms = (time.perf_counter() - t0) * 1000.0
+    e2e_blocking_ms += (args.steps / interval - (W.sort_count - sorts0)) * sort_ms
     clk = clocks.stop()
 
     total_ms, e2e_ms, e2e_blocking_ms = max_over_ranks(torch, [total_ms, e2e_ms, e2e_blocking_ms], world, "cuda")
@@ -735,11 +781,11 @@ def run_ours(args, rank, world):
         if "precision" in wanted:
             extras["precision"] = bench_precision(torch, rsc, synth, dev, steps=min(args.steps, 50))
         if "batch" in wanted:
-            extras["batch"] = bench_batch(torch, rsc, synth, dev, steps=40)
+            extras["batch"] = bench_batch(torch, rsc, synth, dev, steps=500)
         if "les" in wanted:
             extras["les"] = bench_les(torch, rsc, synth, dev, S)
         if "large" in wanted:
-            extras["large"] = bench_large(torch, rsc, synth, dev, chunks=4)
+            extras["large"] = bench_large(torch, rsc, synth, dev, chunks=100)
 
     # CPU baseline: the oracle on a bounded sample of the same workload
     cpu = None
@@ -764,6 +810,11 @@ def run_ours(args, rank, world):
                       "note": "the pulse and the advance of a step run concurrently on two streams; each is "
                               "timed on its own stream, the step from its start to both ends"},
         "compensated": comp,
+        "sort": {"interval_steps": interval, "ms_per_sort": sort_ms, "amortized_ms_per_step": sort_ms / interval,
+                 "sorts_in_value_window": int(sorts_value), "sorts_in_e2e_window": int(sorts_e2e),
+                 "note": "value and e2e include the spatial sort at its amortised cost (ms_per_sort / "
+                         "interval per step): the sorts that fell in each window are replaced by "
+                         "steps / interval of them"},
     }
     line.update(extras)
     print(json.dumps(line))
