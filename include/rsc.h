@@ -40,7 +40,7 @@ extern "C" {
 
 /* pulse-formation precision (additive; the reference has only RSC_PULSE_PLAIN) */
 #define RSC_PULSE_PLAIN 0       /* FP32 exactly as rs.cl scat_sig_aux + pass 1 (gate weights bit-exact) */
-#define RSC_PULSE_COMPENSATED 1 /* FP32 with split range phase, FP64 gate origins, compensated sums */
+#define RSC_PULSE_COMPENSATED 1 /* double-float terms (split range phase), FP64 gate origins, error-free sums */
 #define RSC_PULSE_F64 2         /* FP64 reference of the same FP32 state (error metric oracle) */
 
 typedef struct rsc_worker rsc_worker;
@@ -224,6 +224,10 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
  * pulse blocks per SM leave room for the advance of the same step, which
  * runs beside the pulse on the advance stream. */
 int rsc_set_pulse_shape(rsc_worker *w, int warps, int blocks_per_sm);
+/* Background scatterers per thread of the advance (1 or 2; el_atts and
+ * bg_atts): with 2 a thread forms two scatterers' steps before storing
+ * either, overlapping their dependent loads.  The state is the same. */
+int rsc_set_advance_shape(rsc_worker *w, int scatterers_per_thread);
 
 /* ---- batching form (additive; no counterpart in rs.c) ----
  * A batch runs many emulation instances -- each an rsc_worker with its own
@@ -282,6 +286,16 @@ int rsc_batch_synchronize(rsc_batch *b);
  * (rs.c:2854-2978, rs.c:5188-5200) for batched runs. */
 int rsc_batch_set_les_async(rsc_batch *b, int index, int slot, const float *uvwt4, const float *cpxx4, uint32_t nx,
                             uint32_t ny, uint32_t nz);
+/* The persistent form (additive, off by default): rsc_batch_run and
+ * rsc_batch_run_async then run all steps of every instance in one launch.
+ * Each block owns fixed segments of the instances' scatterers (cut on the
+ * host to equal cost) and, step after step, forms their share of the pulse
+ * and advances them; no block waits for another (the pulses of different
+ * steps use separate accumulators, the last block of an instance's pulse
+ * converting it).  The state and the pulses are the ones of the three-launch
+ * form.  The FP64 precision mode always runs the three-launch form; use_graph
+ * is ignored while this is on. */
+int rsc_batch_set_persistent(rsc_batch *b, int enable);
 /* The largest gate count of the batch (the row length of pulses_out). */
 int rsc_batch_max_gates(rsc_batch *b, int *max_gates);
 /* Kernel launches the batch has issued (per step the pulse, plus the
@@ -460,8 +474,10 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
 /* Diagnostics: evaluate the shared elementary functions (rsmath.h) on the
  * device; fn: 0 sin, 1 cos, 2 log, 3 log1p, 4 acos, 5 atan2(a, b), 6 exp,
  * 7 pow(a, b), 8 the pulse kernel's closed-form range weight of distance a
- * on the triangle table {0, 1, 0} with scale b, origin 1, max 2.  Host
- * arrays of n floats. */
+ * on the triangle table {0, 1, 0} with scale b, origin 1, max 2; 9 / 10
+ * the error (against double) of the compensated pulse's double-float sine /
+ * cosine of the two-way phase b a for a range a and a wave number b,
+ * 11 / 12 the same for the plain FP32 form.  Host arrays of n floats. */
 int rsc_eval_math(int fn, const float *a, const float *b, float *out, size_t n);
 
 #ifdef __cplusplus

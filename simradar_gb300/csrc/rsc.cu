@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <tuple>
 #include <mutex>
 #include <vector>
 
@@ -130,6 +131,7 @@ struct rsc_worker {
     uint64_t launches = 0;
     /* pulse launch shape chosen by rsc_autotune (0: default) */
     int tune_warps = 0, tune_per_sm = 0;
+    int adv_per_thread = 1;   /* background scatterers per advance thread (rsc_set_advance_shape) */
     /* spatial order of the background range (rsc_sort.cuh): perm[slot] is the
      * caller's index, inv[index] the slot; NULL perm = caller's order */
     int sort_interval = 128;
@@ -535,7 +537,18 @@ cudaError_t launch_advance(rsc_worker *w, const AdvanceArgs &a, unsigned blocks,
     }
     if (a.rain_blocks) {
         const bool stretched = rsm_f2u(a.wind[7]) == 7u;   /* the LES index form, fixed per LES */
-        if (a.rain_mode == 1 && stretched) {
+        const unsigned pair_blocks = (unsigned)((a.rain_count + 2 * rsc::kAdvanceThreads - 1) / (2 * rsc::kAdvanceThreads));
+        if (w->adv_per_thread == 2 && a.rain_mode != 2) {
+            if (a.rain_mode == 1 && stretched) {
+                rsc::k_advance_rain2<1, 7><<<pair_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
+            } else if (a.rain_mode == 1) {
+                rsc::k_advance_rain2<1><<<pair_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
+            } else if (stretched) {
+                rsc::k_advance_rain2<0, 7><<<pair_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
+            } else {
+                rsc::k_advance_rain2<0><<<pair_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
+            }
+        } else if (a.rain_mode == 1 && stretched) {
             rsc::k_advance_rain<1, 7><<<a.rain_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
         } else if (a.rain_mode == 1) {
             rsc::k_advance_rain<1><<<a.rain_blocks, rsc::kAdvanceThreads, 0, st>>>(a);
@@ -1528,6 +1541,8 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
     fill_pulse_args(w, P, sim_desc);
     if (mode == RSC_PULSE_COMPENSATED) {
         P.rk = w->rk_hi;
+        /* the error-free warp sums need the grouped path, whatever the order */
+        P.coherent_span = (int)w->G + 1;
     }
     const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
     P.materialize = mat ? 1 : 0;
@@ -1724,6 +1739,17 @@ struct rsc_batch {
     size_t les_stage_n = 0;
     std::vector<cudaEvent_t> slot_used, slot_ready;
     std::vector<char> slot_pending;
+    /* the persistent form (rsc_batch_set_persistent): per-block segments,
+     * per-instance block counts, per-step accumulators and tickets */
+    bool persist = false;
+    unsigned persist_blocks = 0;
+    size_t persist_smem = 0;
+    rsc::PersistSeg *d_pseg = nullptr;
+    unsigned *d_pseg_off = nullptr, *d_pnblk = nullptr;
+    size_t pseg_cap = 0;
+    double *d_pacc = nullptr;
+    unsigned *d_ptick = nullptr;
+    size_t pacc_cap = 0;   /* step x instance slots */
 };
 
 namespace {
@@ -1812,7 +1838,10 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
         acc_d += blocks - A.a.rain_blocks;
         PulseArgs &P = b->h_pulse[i];
         fill_pulse_args(x, P, row[i].sim);
-        if (b->mode == RSC_PULSE_COMPENSATED) P.rk = x->rk_hi;
+        if (b->mode == RSC_PULSE_COMPENSATED) {
+            P.rk = x->rk_hi;
+            P.coherent_span = (int)x->G + 1;
+        }
         P.materialize = 0;
         tri = tri && P.rw_tri;
         /* pulse blocks in proportion to the scatterers, at least one, and no
@@ -2032,6 +2061,16 @@ int rsc_set_pulse_shape(rsc_worker *w, int warps, int blocks_per_sm) {
     return RSC_OK;
 }
 
+int rsc_set_advance_shape(rsc_worker *w, int scatterers_per_thread) {
+    int s = check_worker(w);
+    if (s) return s;
+    if (scatterers_per_thread != 1 && scatterers_per_thread != 2) {
+        return fail(RSC_ERR_ARG, "advance shape: %d scatterers per thread", scatterers_per_thread);
+    }
+    w->adv_per_thread = scatterers_per_thread;
+    return RSC_OK;
+}
+
 int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *blocks_per_sm_out) {
     int s = check_alloc(w);
     if (s) return s;
@@ -2044,7 +2083,10 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
     const int mode = w->precision;
     PulseArgs P;
     fill_pulse_args(w, P, sim_desc);
-    if (mode == RSC_PULSE_COMPENSATED) P.rk = w->rk_hi;
+    if (mode == RSC_PULSE_COMPENSATED) {
+        P.rk = w->rk_hi;
+        P.coherent_span = (int)w->G + 1;
+    }
     P.materialize = 0;
     s = pulse_d2h_wait(w);
     if (s) return s;
@@ -2159,6 +2201,11 @@ int rsc_batch_free(rsc_batch *b) {
     free_ptr(b->d_rain_prefix);
     free_ptr(b->d_deb_prefix);
     free_ptr(b->d_pulse_prefix);
+    free_ptr(b->d_pseg);
+    free_ptr(b->d_pseg_off);
+    free_ptr(b->d_pnblk);
+    free_ptr(b->d_pacc);
+    free_ptr(b->d_ptick);
     if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
     free_ptr(b->les_stage);
     for (cudaEvent_t ev : b->slot_used) {
@@ -2266,6 +2313,175 @@ int rsc_batch_autotune(rsc_batch *b, const float *sim_descs) {
 
 namespace {
 
+/* Cost of one scatterer in the persistent form's partition, in units of a
+ * pulse term: the pulse (1) plus its advance -- a background scatterer's
+ * about one more, a debris scatterer's (attitude, ADM lookups, tumble,
+ * debris RCS) about eight. */
+constexpr double kPersistRainCost = 2.0, kPersistDebrisCost = 9.0, kPersistIdleCost = 1.0;
+
+void *persist_kernel_for(int mode, bool tri) {
+    if (mode == RSC_PULSE_PLAIN) {
+        return tri ? reinterpret_cast<void *>(rsc::k_batch_persist<0, 1>)
+                   : reinterpret_cast<void *>(rsc::k_batch_persist<0, -1>);
+    }
+    return tri ? reinterpret_cast<void *>(rsc::k_batch_persist<1, 1>) : reinterpret_cast<void *>(rsc::k_batch_persist<1, -1>);
+}
+
+/* Cut every instance into segments of equal cost per block (64-aligned
+ * within the instance), one list per block, and size the accumulators for
+ * `steps` steps. */
+int batch_persist_prepare(rsc_batch *b, int steps) {
+    const size_t n = b->w.size();
+    const size_t threads = rsc::kPersistThreads;
+    const size_t smem = (threads / 32) * rsc::pulse_warp_bytes(b->mode, b->Gmax) + 2 * b->Gmax * sizeof(float);
+    void *kern = persist_kernel_for(b->mode, b->tri);
+    if (smem > 48 * 1024) {
+        RSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    int per_sm = 0;
+    RSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)threads, smem));
+    if (per_sm < 1) return fail(RSC_ERR_UNSUPPORTED, "the persistent batch kernel does not fit an SM (%zu B)", smem);
+    if (per_sm > 4) per_sm = 4;
+    const unsigned nb = (unsigned)(b->num_sms * per_sm);
+    /* piecewise-constant cost over each instance's indices */
+    struct Piece {
+        int inst;
+        unsigned long long lo, hi;
+        double w;
+    };
+    std::vector<Piece> pieces;
+    for (size_t i = 0; i < n; i++) {
+        const rsc_worker *x = b->w[i];
+        const rsc_population &pop = b->pops[i];
+        std::vector<std::tuple<unsigned long long, unsigned long long, double>> r;
+        for (int k = 0; k < RSC_MAX_TYPES; k++) {
+            if (pop.counts[k] == 0) continue;
+            r.emplace_back(pop.origins[k], pop.origins[k] + pop.counts[k], k == 0 ? kPersistRainCost : kPersistDebrisCost);
+        }
+        std::sort(r.begin(), r.end());
+        unsigned long long at = 0;
+        for (const auto &q : r) {
+            const unsigned long long lo = std::min<unsigned long long>(std::get<0>(q), x->num_scats);
+            const unsigned long long hi = std::min<unsigned long long>(std::get<1>(q), x->num_scats);
+            if (lo > at) pieces.push_back({(int)i, at, lo, kPersistIdleCost});
+            if (hi > std::max(lo, at)) pieces.push_back({(int)i, std::max(lo, at), hi, std::get<2>(q)});
+            at = std::max(at, hi);
+        }
+        if (at < x->num_scats) pieces.push_back({(int)i, at, x->num_scats, kPersistIdleCost});
+    }
+    double total = 0.0;
+    for (const Piece &p : pieces) total += (double)(p.hi - p.lo) * p.w;
+    const double target = total / nb;
+    std::vector<std::vector<rsc::PersistSeg>> per(nb);
+    unsigned blk = 0;
+    double cum = 0.0;
+    for (const Piece &p : pieces) {
+        unsigned long long cur = p.lo;
+        while (cur < p.hi) {
+            unsigned long long cut = p.hi;
+            if (blk + 1 < nb) {
+                const double room = target * (blk + 1) - cum;
+                const unsigned long long take = room <= 0.0 ? 0 : (unsigned long long)ceil(room / p.w);
+                const unsigned long long c = ((cur + take + 63) / 64) * 64;   /* 64-aligned in the instance */
+                if (c < p.hi) cut = std::max(c, cur + 1);
+            }
+            auto &v = per[blk];
+            if (!v.empty() && v.back().inst == p.inst && v.back().end == cur) {
+                v.back().end = cut;
+            } else {
+                v.push_back({cur, cut, p.inst, 0});
+            }
+            cum += (double)(cut - cur) * p.w;
+            cur = cut;
+            if (blk + 1 < nb && cum >= target * (blk + 1) - 1e-9) blk++;
+        }
+    }
+    std::vector<rsc::PersistSeg> seg;
+    std::vector<unsigned> off(nb + 1, 0u), nblk(n, 0u);
+    for (unsigned q = 0; q < nb; q++) {
+        off[q] = (unsigned)seg.size();
+        int last = -1;
+        for (const auto &g : per[q]) {
+            seg.push_back(g);
+            if (g.inst != last) nblk[g.inst]++;
+            last = g.inst;
+        }
+    }
+    off[nb] = (unsigned)seg.size();
+    for (size_t i = 0; i < n; i++) {
+        if (nblk[i] == 0) return fail(RSC_ERR_STATE, "persistent partition left instance %zu without a block", i);
+    }
+    if (seg.size() > b->pseg_cap || b->d_pseg_off == nullptr) {
+        free_ptr(b->d_pseg);
+        free_ptr(b->d_pseg_off);
+        free_ptr(b->d_pnblk);
+        b->pseg_cap = 0;
+        cudaError_t e = cudaMalloc((void **)&b->d_pseg, seg.size() * sizeof(rsc::PersistSeg));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pseg_off, (size_t)(4 * b->num_sms + 1) * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pnblk, n * sizeof(unsigned));
+        if (e != cudaSuccess) return cuda_fail(RSC_ERR_NOMEM, "persistent segments: %s", cudaGetErrorString(e));
+        b->pseg_cap = seg.size();
+    }
+    const size_t slots = (size_t)steps * n;
+    if (slots > b->pacc_cap) {
+        free_ptr(b->d_pacc);
+        free_ptr(b->d_ptick);
+        b->pacc_cap = 0;
+        cudaError_t e = cudaMalloc((void **)&b->d_pacc, slots * b->Gmax * 4 * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_ptick, slots * sizeof(unsigned));
+        if (e != cudaSuccess) return cuda_fail(RSC_ERR_NOMEM, "persistent accumulators: %s", cudaGetErrorString(e));
+        b->pacc_cap = slots;
+    }
+    RSC_CUDA(cudaMemcpyAsync(b->d_pseg, seg.data(), seg.size() * sizeof(rsc::PersistSeg), cudaMemcpyHostToDevice,
+                             b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_pseg_off, off.data(), off.size() * sizeof(unsigned), cudaMemcpyHostToDevice,
+                             b->stream));
+    RSC_CUDA(cudaMemcpyAsync(b->d_pnblk, nblk.data(), n * sizeof(unsigned), cudaMemcpyHostToDevice, b->stream));
+    /* the copies read host vectors of this call: wait before they go */
+    RSC_CUDA(cudaStreamSynchronize(b->stream));
+    b->persist_blocks = nb;
+    b->persist_smem = smem;
+    return RSC_OK;
+}
+
+/* Every step of the run in one launch (after zeroing its accumulators). */
+int batch_persist_launch(rsc_batch *b, int steps) {
+    const size_t n = b->w.size();
+    const size_t slots = (size_t)steps * n;
+    RSC_CUDA(cudaMemsetAsync(b->d_pacc, 0, slots * b->Gmax * 4 * sizeof(double), b->stream));
+    RSC_CUDA(cudaMemsetAsync(b->d_ptick, 0, slots * sizeof(unsigned), b->stream));
+    rsc::PersistArgs A;
+    memset(&A, 0, sizeof(A));
+    A.adv = b->d_adv;
+    A.pulse = b->d_pulse;
+    A.steps = b->d_steps;
+    A.seg = b->d_pseg;
+    A.seg_off = b->d_pseg_off;
+    A.nblk = b->d_pnblk;
+    A.acc = b->d_pacc;
+    A.tick = b->d_ptick;
+    A.out = b->d_out;
+    A.out_stride = b->Gmax;
+    A.Gmax = b->Gmax;
+    A.steps_n = steps;
+    A.ninst = (int)n;
+    const unsigned g = b->persist_blocks;
+    const size_t sm = b->persist_smem;
+    const unsigned t = rsc::kPersistThreads;
+    if (b->mode == RSC_PULSE_PLAIN && b->tri) {
+        rsc::k_batch_persist<0, 1><<<g, t, sm, b->stream>>>(A);
+    } else if (b->mode == RSC_PULSE_PLAIN) {
+        rsc::k_batch_persist<0, -1><<<g, t, sm, b->stream>>>(A);
+    } else if (b->tri) {
+        rsc::k_batch_persist<1, 1><<<g, t, sm, b->stream>>>(A);
+    } else {
+        rsc::k_batch_persist<1, -1><<<g, t, sm, b->stream>>>(A);
+    }
+    RSC_CUDA(cudaGetLastError());
+    b->launches += 1;
+    return RSC_OK;
+}
+
 int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_ids, float *pulses_out, int use_graph,
               bool wait) {
     int s = check_batch(b);
@@ -2313,16 +2529,21 @@ int batch_run(rsc_batch *b, int steps, const float *sim_descs, const int *les_id
     RSC_CUDA(cudaMemcpyAsync(b->d_steps, b->h_steps, (size_t)steps * n * sizeof(rsc::BatchStep),
                              cudaMemcpyHostToDevice, b->stream));
     RSC_CUDA(cudaEventRecord(b->ev_h2d, b->stream));
-    if (use_graph) {
+    if (b->persist && b->mode != RSC_PULSE_F64) {
+        s = batch_persist_prepare(b, steps);
+        if (s == RSC_OK) s = batch_persist_launch(b, steps);
+        if (s) return s;
+    } else if (use_graph) {
         if (b->graph == nullptr || b->graph_steps != steps) {
             s = batch_capture(b, steps);
             if (s) return s;
         }
         RSC_CUDA(cudaGraphLaunch(b->graph, b->stream));
+        b->launches += (uint64_t)steps * (1u + (b->rain_blocks ? 1u : 0u) + (b->deb_blocks ? 1u : 0u));
     } else {
         RSC_CUDA(batch_enqueue(b, steps));
+        b->launches += (uint64_t)steps * (1u + (b->rain_blocks ? 1u : 0u) + (b->deb_blocks ? 1u : 0u));
     }
-    b->launches += (uint64_t)steps * (1u + (b->rain_blocks ? 1u : 0u) + (b->deb_blocks ? 1u : 0u));
     batch_swap_pairs(b, steps);
     for (size_t q = 0; q < 2 * n; q++) {
         if (used[q]) RSC_CUDA(cudaEventRecord(b->slot_used[q], b->stream));
@@ -2420,6 +2641,12 @@ int rsc_batch_launch_count(rsc_batch *b, uint64_t *count) {
 int rsc_batch_get_stream(rsc_batch *b, void **stream) {
     if (b == nullptr || stream == nullptr) return fail(RSC_ERR_ARG, "NULL argument");
     *stream = (void *)b->stream;
+    return RSC_OK;
+}
+
+int rsc_batch_set_persistent(rsc_batch *b, int enable) {
+    if (b == nullptr) return fail(RSC_ERR_ARG, "batch is NULL");
+    b->persist = enable != 0;
     return RSC_OK;
 }
 
@@ -2624,7 +2851,11 @@ int rsc_eval_math(int fn, const float *a, const float *b, float *out, size_t n) 
     RSC_CUDA(cudaMalloc((void **)&dout, n * sizeof(float)));
     RSC_CUDA(cudaMemcpy(da, a, n * sizeof(float), cudaMemcpyHostToDevice));
     RSC_CUDA(cudaMemcpy(db, b ? b : a, n * sizeof(float), cudaMemcpyHostToDevice));
-    rsc::k_eval_math<<<(unsigned)((n + 255) / 256), 256>>>(fn, da, db, dout, n);
+    if (fn >= 9 && fn <= 12) {
+        rsc::k_eval_phase<<<(unsigned)((n + 255) / 256), 256>>>(fn, da, db, dout, n);
+    } else {
+        rsc::k_eval_math<<<(unsigned)((n + 255) / 256), 256>>>(fn, da, db, dout, n);
+    }
     RSC_CUDA(cudaGetLastError());
     RSC_CUDA(cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost));
     cudaFree(da);

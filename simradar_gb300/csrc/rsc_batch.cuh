@@ -158,6 +158,143 @@ k_pulse_batch(const PulseArgs *inst, const BatchStep *steps, const unsigned *pre
     }
 }
 
+/* ---- every step of a run in one launch (the persistent form) ----
+ * Each block owns a fixed list of segments -- contiguous index ranges of an
+ * instance, cut by the host so that every block carries the same cost --
+ * and runs every step of the run on them: the segment's share of the
+ * instance's pulse (its bins summed into that step's accumulator of the
+ * instance, the last of the instance's blocks converting it), then the
+ * advance of the same scatterers into the step's other pos / rcs pair.  The
+ * pulse of step k + 1 reads only what this block's advance of step k wrote
+ * and the advance of step k + 1 overwrites only what this block's pulse of
+ * step k read, so no block ever waits for another: the pulses of different
+ * steps use different accumulators and tickets ([step][instance]).  State is
+ * read by the pulse with L2 loads (ld.global.cg): the arrays change during
+ * the launch, so the read-only (non-coherent) path may not serve them. */
+struct PersistSeg {
+    unsigned long long start, end;   /* [start, end) of instance `inst` */
+    int inst;
+    int pad;
+};
+
+struct PersistArgs {
+    const BatchAdvance *adv;
+    const PulseArgs *pulse;
+    const BatchStep *steps;          /* [k][instance] */
+    const PersistSeg *seg;           /* the segments of block b: seg[seg_off[b] .. seg_off[b + 1]) */
+    const unsigned *seg_off;
+    const unsigned *nblk;            /* per instance: the blocks whose segments cover it */
+    double *acc;                     /* [k][instance][Gmax][4], zero at launch */
+    unsigned *tick;                  /* [k][instance], zero at launch */
+    float4 *out;                     /* [k][instance][out_stride] */
+    unsigned out_stride, Gmax;
+    int steps_n, ninst;
+};
+
+constexpr int kPersistThreads = 256;
+
+/* The pulse share of [start, end): runs of 64 neighbours per warp, two per
+ * lane (PulseBins::add_k), then the block's sums into the accumulator. */
+template <int MODE, int TRI>
+__device__ __forceinline__ void persist_pulse(const PulseArgs &P, unsigned long long start, unsigned long long end,
+                                              unsigned nblk) {
+    PulseBins<MODE, 1> B;
+    B.init(P);
+    const unsigned long long stride = 64ull * (blockDim.x >> 5);
+    for (unsigned long long base = start + 64ull * B.warp; base < end; base += stride) {
+        bool in[2];
+        unsigned long long idx[2];
+        float4 pp[2], xx[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            idx[q] = base + 32u * q + B.lane;
+            in[q] = idx[q] < end;
+            pp[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            xx[q] = pp[q];
+            if (in[q]) {
+                pp[q] = __ldcg(P.pos + idx[q]);
+                xx[q] = __ldcg(P.rcs + idx[q]);
+            }
+        }
+        B.template add_k<2, TRI>(P, in, idx, pp, xx);
+    }
+    B.finish(P, nblk);
+}
+
+/* The advance of [start, end): the background body of the instance's
+ * concept inside the background range, db_atts inside a debris range. */
+__device__ __forceinline__ void persist_advance(const AdvanceArgs &a, unsigned long long start, unsigned long long end) {
+    const unsigned long long r0 = a.rain_origin, r1 = a.rain_origin + a.rain_count;
+    for (unsigned long long x = start + threadIdx.x; x < end; x += blockDim.x) {
+        float4 pos, rcs;
+        bool known;
+        if (x >= r0 && x < r1) {
+            if (a.rain_mode == 1) {
+                rain_el(a, (size_t)x, pos, rcs, known);
+            } else if (a.rain_mode == 0) {
+                rain_bg(a, (size_t)x, pos, rcs, known);
+            } else {
+                rain_fp(a, (size_t)x, pos, rcs, known);
+            }
+            continue;
+        }
+        for (int t = 0; t < a.ntypes; t++) {
+            const DebrisType &T = a.types[t];
+            if (x >= T.origin && x < T.origin + T.count) {
+                debris_step(a, T, (size_t)x, pos, rcs, known);
+                break;
+            }
+        }
+    }
+}
+
+template <int MODE, int TRI = -1>
+__global__ void __launch_bounds__(kPersistThreads, 4) k_batch_persist(const PersistArgs A) {
+    __shared__ __align__(16) PulseArgs sp;
+    __shared__ __align__(16) AdvanceArgs sa;
+    const unsigned s0 = __ldg(A.seg_off + blockIdx.x), s1 = __ldg(A.seg_off + blockIdx.x + 1);
+    for (int k = 0; k < A.steps_n; k++) {
+        for (unsigned sg = s0; sg < s1; sg++) {
+            const int i = A.seg[sg].inst;
+            const unsigned long long start = A.seg[sg].start, end = A.seg[sg].end;
+            const size_t slot = (size_t)k * A.ninst + i;
+            const BatchStep *st = A.steps + slot;
+            /* the pulse of step k on this segment */
+            block_copy(&sp, &A.pulse[i], sizeof(PulseArgs));
+            __syncthreads();
+            if (threadIdx.x < 16) sp.sim[threadIdx.x] = st->sim[threadIdx.x];
+            if (threadIdx.x == 0) {
+                sp.pulse = A.out + slot * A.out_stride;
+                sp.acc64 = A.acc + slot * A.Gmax * 4;
+                sp.counter = A.tick + slot;
+                sp.pos = st->pos_r;
+                sp.rcs = st->rcs_r;
+                beam_norm_df(st->sim, sp.bn_hi, sp.bn_lo);
+            }
+            __syncthreads();
+            persist_pulse<MODE, TRI>(sp, start, end, __ldg(A.nblk + i));
+            __syncthreads();
+            /* then its advance into the step's other pair */
+            block_copy(&sa, &A.adv[i].a, sizeof(AdvanceArgs));
+            __syncthreads();
+            if (threadIdx.x < 16) sa.sim[threadIdx.x] = st->sim[threadIdx.x];
+            if (threadIdx.x == 0) {
+                const int les = st->les_id & 1;
+                sa.uvwt = A.adv[i].uvwt[les];
+                sa.cpxx = A.adv[i].cpxx[les];
+                sa.dff = A.adv[i].dff[les];
+                sa.pos_in = st->pos_r;
+                sa.rcs_in = st->rcs_r;
+                sa.pos = st->pos_w;
+                sa.rcs = st->rcs_w;
+            }
+            __syncthreads();
+            persist_advance(sa, start, end);
+            __syncthreads();
+        }
+    }
+}
+
 }  // namespace rsc
 
 #endif

@@ -54,9 +54,51 @@ struct AdvanceArgs {
     DebrisType types[RSC_MAX_TYPES - 1];
 };
 
+/* What one background step makes of a scatterer, formed before anything is
+ * stored, so that a thread can carry two scatterers' dependent load chains
+ * (state, then LES texels) at once.  On a respawn `rcs` is the stored
+ * backscatter, which the step keeps. */
+struct RainNext {
+    float4 pos, vel, rcs;
+    uint4 seed;
+    bool respawn;
+};
+
+__device__ __forceinline__ void rain_store(const AdvanceArgs &a, size_t i, const RainNext &o) {
+    a.pos[i] = o.pos;
+    a.vel[i] = o.vel;
+    if (o.respawn) {
+        /* the only time the seed is written; rcs keeps its previous value */
+        a.rnd[i] = o.seed;
+        if (a.rcs != a.rcs_in) a.rcs[i] = o.rcs;
+    } else {
+        a.rcs[i] = o.rcs;
+    }
+}
+
+/* respawn (rs.cl:546-556, rs.cl:668-678): the only time the seed is read */
+template <bool FMA>
+__device__ __forceinline__ void rain_respawn(const AdvanceArgs &a, size_t i, const float *sd, RainNext &o) {
+    uint4 seed = a.rnd[i];
+    float4 r = cl_rand(&seed);
+    if (FMA) {
+        o.pos.x = fmaf(r.x, sd[12], sd[8]);
+        o.pos.y = fmaf(r.y, sd[13], sd[9]);
+        o.pos.z = fmaf(r.z, sd[14], sd[10]);
+    } else {
+        o.pos.x = r.x * sd[12] + sd[8];
+        o.pos.y = r.y * sd[13] + sd[9];
+        o.pos.z = r.z * sd[14] + sd[10];
+    }
+    o.vel = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    o.seed = seed;
+    o.rcs = a.rcs_in[i];
+    o.respawn = true;
+}
+
 /* ---- el_atts (rs.cl:653-739) ---- */
 template <int SP = -1>
-__device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
+__device__ __forceinline__ void rain_el_next(const AdvanceArgs &a, size_t i, RainNext &o) {
     const float *sd = a.sim;
     const float dt = sd[11];
     const uint32_t concept = __float_as_uint(sd[5]);
@@ -69,20 +111,9 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
     pos.z = fmaf(vel.z, dt, pos.z);
     pos.w = fmaf(vel.w, 0.0f, pos.w);
     const float area_over_mass_particle = 0.003006012f / pos.w;
+    o.pos = pos;
     if (is_outside(pos, sd)) {
-        /* respawn: the only time the seed is read or written, and rcs keeps
-         * its previous value (el_atts writes x[i] = rcs unchanged) */
-        uint4 seed = a.rnd[i];
-        float4 r = cl_rand(&seed);
-        pos.x = fmaf(r.x, sd[12], sd[8]);
-        pos.y = fmaf(r.y, sd[13], sd[9]);
-        pos.z = fmaf(r.z, sd[14], sd[10]);
-        a.pos[i] = pos;
-        a.vel[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
-        a.rnd[i] = seed;
-        if (a.rcs != a.rcs_in) a.rcs[i] = a.rcs_in[i];
-        po = pos;
-        xk = false;
+        rain_respawn<true>(a, i, sd, o);
         return;
     }
     float4 bg_vel = compute_bg_vel<SP>(pos, a.uvwt, a.wind, sd);
@@ -110,18 +141,14 @@ __device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &
         vel.z = vel.z + g_dt;
         vel.w = vel.w + 0.0f * 0.0f;
     }
-    float4 rcs = compute_ellipsoid_rcs(pos, a.drop, a.drop_desc);
-    a.pos[i] = pos;
-    a.vel[i] = vel;
-    a.rcs[i] = rcs;
-    po = pos;
-    xo = rcs;
-    xk = true;
+    o.vel = vel;
+    o.rcs = compute_ellipsoid_rcs(pos, a.drop, a.drop_desc);
+    o.respawn = false;
 }
 
 /* ---- bg_atts (rs.cl:533-580) ---- */
 template <int SP = -1>
-__device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
+__device__ __forceinline__ void rain_bg_next(const AdvanceArgs &a, size_t i, RainNext &o) {
     const float *sd = a.sim;
     const float dt = sd[11];
     float4 pos = a.pos_in[i];
@@ -130,28 +157,36 @@ __device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &
     pos.y = pos.y + vel.y * dt;
     pos.z = pos.z + vel.z * dt;
     pos.w = pos.w + vel.w * 0.0f;
+    o.pos = pos;
     if (is_outside(pos, sd)) {
-        uint4 seed = a.rnd[i];
-        float4 r = cl_rand(&seed);
-        pos.x = r.x * sd[12] + sd[8];
-        pos.y = r.y * sd[13] + sd[9];
-        pos.z = r.z * sd[14] + sd[10];
-        a.pos[i] = pos;
-        a.vel[i] = f4(0.0f, 0.0f, 0.0f, 0.0f);
-        a.rnd[i] = seed;
-        if (a.rcs != a.rcs_in) a.rcs[i] = a.rcs_in[i];
-        po = pos;
-        xk = false;
+        rain_respawn<false>(a, i, sd, o);
         return;
     }
-    vel = compute_bg_vel<SP>(pos, a.uvwt, a.wind, sd);
-    float4 rcs = compute_ellipsoid_rcs(pos, a.drop, a.drop_desc);
-    a.pos[i] = pos;
-    a.vel[i] = vel;
-    a.rcs[i] = rcs;
-    po = pos;
-    xo = rcs;
-    xk = true;
+    o.vel = compute_bg_vel<SP>(pos, a.uvwt, a.wind, sd);
+    o.rcs = compute_ellipsoid_rcs(pos, a.drop, a.drop_desc);
+    o.respawn = false;
+}
+
+/* The background step of scatterer i, stored; its new position and
+ * backscatter returned (xk false on a respawn, where xo is the kept one). */
+template <int SP = -1>
+__device__ __forceinline__ void rain_el(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
+    RainNext o;
+    rain_el_next<SP>(a, i, o);
+    rain_store(a, i, o);
+    po = o.pos;
+    xo = o.rcs;
+    xk = !o.respawn;
+}
+
+template <int SP = -1>
+__device__ __forceinline__ void rain_bg(const AdvanceArgs &a, size_t i, float4 &po, float4 &xo, bool &xk) {
+    RainNext o;
+    rain_bg_next<SP>(a, i, o);
+    rain_store(a, i, o);
+    po = o.pos;
+    xo = o.rcs;
+    xk = !o.respawn;
 }
 
 /* ---- fp_atts (rs.cl:590-648) ---- */
@@ -325,7 +360,6 @@ __device__ __forceinline__ bool advance_one_t(const AdvanceArgs &a, unsigned b, 
         } else {
             rain_fp(a, i, pos, rcs, known);
         }
-        if (!known) rcs = a.rcs_in[i];   /* respawned: the stored backscatter stays */
         i_out = i;
         return true;
     }
@@ -367,6 +401,33 @@ __global__ void __launch_bounds__(kAdvanceThreads, 2048 / kAdvanceThreads) k_adv
         rain_bg<SP>(a, i, pos, rcs, known);
     } else {
         rain_fp(a, i, pos, rcs, known);
+    }
+}
+
+/* The same step with two scatterers per thread (j and j + 128 of a block of
+ * 256 scatterers): both are formed before either is stored, so the loads of
+ * the two dependent chains overlap in one thread.  el_atts / bg_atts only. */
+template <int RAIN_MODE, int SP = -1>
+__global__ void __launch_bounds__(kAdvanceThreads, 1024 / kAdvanceThreads) k_advance_rain2(const AdvanceArgs a) {
+    static_assert(RAIN_MODE == 0 || RAIN_MODE == 1, "el_atts / bg_atts");
+    const unsigned long long j0 = (unsigned long long)blockIdx.x * (2 * kAdvanceThreads) + threadIdx.x;
+    RainNext o[2];
+    bool in[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const unsigned long long j = j0 + (unsigned long long)q * kAdvanceThreads;
+        in[q] = j < a.rain_count;
+        if (in[q]) {
+            if (RAIN_MODE == 1) {
+                rain_el_next<SP>(a, (size_t)(a.rain_origin + j), o[q]);
+            } else {
+                rain_bg_next<SP>(a, (size_t)(a.rain_origin + j), o[q]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (in[q]) rain_store(a, (size_t)(a.rain_origin + j0 + (unsigned long long)q * kAdvanceThreads), o[q]);
     }
 }
 
@@ -490,6 +551,16 @@ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
     p = a * b;
     e = fmaf(a, b, -p);
 }
+/* a + b = s + e exactly, for |a| >= |b| (or a == 0) */
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    e = b - (s - a);
+}
+/* (ah + al)(bh + bl) as a double-float pair (unnormalised), dropping al bl */
+__device__ __forceinline__ void df_mul_pair(float ah, float al, float bh, float bl, float &h, float &l) {
+    h = ah * bh;
+    l = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -h)));
+}
 
 /* accumulators: per-warp gate bins in shared memory */
 struct AccF32 {
@@ -507,19 +578,28 @@ struct AccF32 {
 };
 
 /* double-float bin: 4 heads then 4 tails */
+/* double-float contributions: heads v, tails u */
 struct AccDF {
     typedef float bin_t;
     static constexpr int kWords = 2;
-    float v[4];
-    __device__ void set(float a, float b, float c, float d) { v[0] = a; v[1] = b; v[2] = c; v[3] = d; }
-    __device__ void scale(float w, AccDF &o) const { o.set(w * v[0], w * v[1], w * v[2], w * v[3]); }
+    float v[4], u[4];
+    __device__ void set(float a, float b, float c, float d) {
+        v[0] = a; v[1] = b; v[2] = c; v[3] = d;
+        u[0] = u[1] = u[2] = u[3] = 0.0f;
+    }
+    __device__ void set_lo(const float *t) { u[0] = t[0]; u[1] = t[1]; u[2] = t[2]; u[3] = t[3]; }
+    __device__ void scale(float w, AccDF &o) const { scale_df(w, 0.0f, o); }
+    __device__ void scale_df(float wh, float wl, AccDF &o) const {
+#pragma unroll
+        for (int l = 0; l < 4; l++) df_mul_pair(v[l], u[l], wh, wl, o.v[l], o.u[l]);
+    }
     __device__ static void add_to(float *bin, const AccDF &c) {
 #pragma unroll
         for (int l = 0; l < 4; l++) {
             float s, e;
             two_sum(bin[l], c.v[l], s, e);
             bin[l] = s;
-            bin[4 + l] = bin[4 + l] + e;
+            bin[4 + l] = bin[4 + l] + (e + c.u[l]);
         }
     }
 };
@@ -562,7 +642,7 @@ __device__ __forceinline__ void bin_add(typename Acc::bin_t *wbins, unsigned act
 template <class Acc>
 __device__ __forceinline__ void warp_sum_into(typename Acc::bin_t *bin, Acc c) {
     if constexpr (Acc::kWords == 2) {
-        float lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float lo[4] = {c.u[0], c.u[1], c.u[2], c.u[3]};
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
 #pragma unroll
@@ -600,6 +680,7 @@ struct Sig32 {
     float r, g;          /* range and fractional gate position */
     float r_lo;          /* compensated: tail of the range */
     AccF32 s;            /* sig * angular weight */
+    float s_lo[4];       /* compensated: the tails of s (s + s_lo as double-floats) */
     float sig[4];        /* sig before the angular weight (for aux/sig output) */
     float wang;
 };

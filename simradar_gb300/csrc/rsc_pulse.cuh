@@ -11,12 +11,12 @@
  *
  *   RSC_PULSE_PLAIN        FP32 throughout, as the reference; per-warp bins
  *                          updated with shared-memory atomics.
- *   RSC_PULSE_COMPENSATED  range, beam angle and gate offsets as double-floats,
- *                          split range phase, FP64 gate origins, table indices
- *                          with their rounding error carried; contributions go
- *                          into FP32 per-warp bins that the warp folds into
- *                          double-float bins after every 32 scatterers, and the
- *                          block and grid sums stay double-float.
+ *   RSC_PULSE_COMPENSATED  every factor of a term as a double-float (range,
+ *                          beam angle, table lerps, split range phase and its
+ *                          sine and cosine, 1 / r^2, rotation), FP64 gate
+ *                          origins; the warp sums each gate with an error-free
+ *                          butterfly into double-float bins, the block sums
+ *                          double-float and the grid FP64.
  *   RSC_PULSE_F64          FP64 reference of the same FP32 state: per-warp
  *                          FP64 bins, lanes on the same gate serialised.
  *
@@ -27,6 +27,7 @@
 #define SIMRADAR_GB300_RSC_PULSE_CUH
 
 #include "rsc_kernels.cuh"
+#include "rsc_sincos_table.h"
 
 namespace rsc {
 
@@ -69,6 +70,71 @@ __device__ __forceinline__ float range_weight_comp(const float *W, const float *
     const float pe = fmaf(a_hi, s, -p) + a_lo * s;
     const float sg = (p + pe) < 0.0f ? -1.0f : 1.0f;
     return fmaxf((1.0f - sg * p) - sg * pe, 0.0f);
+}
+
+/* weight_comp as a double-float (wh + wl): the fraction (f - fl) + fe kept
+ * as a pair (f - fl is exact), the table difference w1 - w0 exact
+ * (two_sum), their product and the sum with w0 error-free but for the
+ * product of the tails -- the lerp of the FP32 table at the double-float
+ * index, to ~1e-14 of the weight. */
+__device__ __forceinline__ void weight_comp_df(const float *W, const float *desc, float a_hi, float a_lo, float &wh,
+                                               float &wl) {
+    const float s = desc[0], o = desc[1], m = desc[2];
+    float p = a_hi * s;
+    float pe = fmaf(a_hi, s, -p) + a_lo * s;
+    float f, fe;
+    two_sum(p, o, f, fe);
+    fe = fe + pe;
+    const float fsum = f + fe;
+    wl = 0.0f;
+    if (!(fsum > 0.0f)) {
+        wh = __ldg(W);
+        return;
+    }
+    if (fsum >= m) {
+        wh = __ldg(W + (int)m);
+        return;
+    }
+    const float fl = floorf(fsum);
+    float fh = f - fl, fr = fe;
+    const float ft = fh + fr;
+    if (ft <= 0.0f) {
+        fh = 0.0f;
+        fr = 0.0f;
+    } else if (ft >= 1.0f) {
+        fh = 1.0f;
+        fr = 0.0f;
+    }
+    const int i0 = (int)fl;
+    const int i1 = min(i0 + 1, (int)m);
+    const float w0 = __ldg(W + i0), w1 = __ldg(W + i1);
+    float dh, dl;
+    two_sum(w1, -w0, dh, dl);
+    float ph, pl;
+    df_mul_pair(dh, dl, fh, fr, ph, pl);
+    float sh, se;
+    two_sum(w0, ph, sh, se);
+    fast_two_sum(sh, se + pl, wh, wl);
+}
+
+/* range_weight_comp as a double-float: on the triangle 1 - |t| with the
+ * head 1 - sg p formed error-free. */
+__device__ __forceinline__ void range_weight_comp_df(const float *W, const float *desc, int tri, float a_hi, float a_lo,
+                                                     float &wh, float &wl) {
+    if (!tri) {
+        weight_comp_df(W, desc, a_hi, a_lo, wh, wl);
+        return;
+    }
+    const float s = desc[0];
+    const float p = a_hi * s;
+    const float pe = fmaf(a_hi, s, -p) + a_lo * s;
+    const float sg = (p + pe) < 0.0f ? -1.0f : 1.0f;
+    float h, e;
+    two_sum(1.0f, -sg * p, h, e);
+    const float l = e - sg * pe;
+    const bool pos = (h + l) > 0.0f;
+    wh = pos ? h : 0.0f;
+    wl = pos ? l : 0.0f;
 }
 
 /* double-float helpers: (hi, lo) with |lo| <= ulp(hi) / 2 */
@@ -132,12 +198,173 @@ __device__ __forceinline__ void df_norm2_f(const float *h3, float &h, float &l) 
     l = sl;
 }
 
-/* compensated signal.  Range r = |p| and the beam angle are double-floats
- * from the FP32 position: the angle is asin(|b x p| / (|b| |p|)) with the
- * cross product formed exactly (two_prod) and the asin series (rsmath.h)
- * applied to the small correction only, so its error stays near 1e-12 where
- * the antenna table can see it (< 15.5 deg).  The phase k r is reduced by
- * pi/2 with k * r_hi split exactly and the tails added after reduction. */
+/* x - q pi/2 as a double-float for x = xh + xsh + xsl, with xh an FP32
+ * value and xsh + xsl a small double-float (|xsh| < 1: the tails of a
+ * split product), q the integer nearest to x 2/pi.  q is found from x 2/pi
+ * formed as a double-float (2/pi in two parts, the head product exact): a
+ * single FP32 product rounds to a quarter near 4e6 rad (the phase at 30 km)
+ * and 2/pi in one float is off by 4e-8 of it, which together can leave q
+ * one off.  xh - q RSM_PIO2_1 is exact (xh is a multiple of the ulp of
+ * RSM_PIO2_1, or q is 0 or 1, and the difference is below 1 in magnitude,
+ * for |xh| < 2^22); q RSM_PIO2_2 is subtracted as an exact product and xsh
+ * added error-free, so only the terms below 1e-7 (the product errors, the
+ * third part of pi/2 and xsl) are rounded: the result is within ~1e-15 rad
+ * of x - q pi/2 whatever the size of x. */
+__device__ __forceinline__ void reduce_pio2_df(float xh, float xsh, float xsl, float &q, float &rh, float &rl) {
+    float ph, pl;
+    two_prod(xh, RSM_TWO_OVER_PI, ph, pl);
+    pl = fmaf(xh, 0x1.b93910p-26f, pl) + xsh * RSM_TWO_OVER_PI;   /* 2/pi - RSM_TWO_OVER_PI */
+    const float q0 = rintf(ph);
+    const float fr = (ph - q0) + pl;
+    q = fr > 0.5f ? q0 + 1.0f : (fr < -0.5f ? q0 - 1.0f : q0);
+    const float r1 = fmaf(-q, RSM_PIO2_1, xh);
+    float th, tl;
+    two_prod(q, RSM_PIO2_2, th, tl);
+    float s, e, s2, e2;
+    two_sum(r1, -th, s, e);
+    two_sum(s, xsh, s2, e2);
+    const float tail = e2 + ((e - tl) + fmaf(-q, RSM_PIO2_3, xsl));
+    two_sum(s2, tail, rh, rl);
+}
+
+/* sine and cosine of the double-float r = rh + rl (|r| <= pi/4 + 1e-6)
+ * plus q pi/2, as double-floats accurate to ~1e-14.  With t = j/64 the
+ * nearest node and d = r - t (|d| <= 1/128; rh - t is exact):
+ *   sin(t + d) = S + (S m + C sd),  cos(t + d) = C + (C m - S sd),
+ *   sd = sin d = d - d^3/6 + d^5/120,  m = cos d - 1 = -d^2/2 + d^4/24,
+ * S, C the node's sine and cosine as double-floats (kSinCosNode, exact to
+ * 2^-48).  Past their first terms the series are below 8e-8 (sd) and
+ * 1.6e-10 (m) and are formed in FP32; d^2 is split exactly.  The terms
+ * dropped (d^7/5040, d^6/720) are below 1e-18. */
+__device__ __forceinline__ void sincos_df(float rh, float rl, float q, float &sh, float &sl, float &ch, float &cl) {
+    const float jf = rintf(rh * kSinCosStep);
+    const float dh = fmaf(-jf, 1.0f / kSinCosStep, rh);
+    const int j = (int)jf;
+    const float4 T = __ldg(&kSinCosNode[min(abs(j), kSinCosNodes - 1)]);
+    const float Sh = j < 0 ? -T.x : T.x, Sl = j < 0 ? -T.y : T.y;
+    const float Ch = T.z, Cl = T.w;
+    /* d^2 = p + pe (exact head product, tail with 2 dh rl) */
+    float p, pe;
+    two_prod(dh, dh, p, pe);
+    pe = fmaf(2.0f * dh, rl, pe);
+    const float mh = -0.5f * p;
+    const float ml = fmaf(0x1.555556p-5f * p, p, -0.5f * pe);   /* d^4/24 - pe/2 */
+    /* sd = dh + (rl + c3), c3 = -dh^3/6 + dh^5/120 - dh^2 rl/2 */
+    const float c3 = fmaf(dh * p, fmaf(p, 0x1.111112p-7f, -0x1.555556p-3f), -0.5f * p * rl);
+    const float sdl = rl + c3;
+    float Ah, Al, Bh, Bl, Dh, Dl, Eh, El;
+    df_mul_pair(Sh, Sl, mh, ml, Ah, Al);    /* S m */
+    df_mul_pair(Ch, Cl, dh, sdl, Bh, Bl);   /* C sd */
+    df_mul_pair(Ch, Cl, mh, ml, Dh, Dl);    /* C m */
+    df_mul_pair(Sh, Sl, dh, sdl, Eh, El);   /* S sd */
+    float u, ue, v, ve;
+    two_sum(Ah, Bh, u, ue);
+    two_sum(Sh, u, v, ve);
+    float s0h, s0l, c0h, c0l;
+    fast_two_sum(v, ve + (ue + Al + Bl + Sl), s0h, s0l);
+    two_sum(Dh, -Eh, u, ue);
+    two_sum(Ch, u, v, ve);
+    fast_two_sum(v, ve + (ue + Dl - El + Cl), c0h, c0l);
+    /* quadrant (as rsm_sincos_reduced): (s, c), (c, -s), (-s, -c), (-c, s) */
+    const int quad = (int)q & 3;
+    const bool swap = (quad & 1) != 0;
+    const float a_h = swap ? c0h : s0h, a_l = swap ? c0l : s0l;
+    const float b_h = swap ? s0h : c0h, b_l = swap ? s0l : c0l;
+    const bool ns = (quad & 2) != 0, nc = ((quad + 1) & 2) != 0;
+    sh = ns ? -a_h : a_h;
+    sl = ns ? -a_l : a_l;
+    ch = nc ? -b_h : b_h;
+    cl = nc ? -b_l : b_l;
+}
+
+/* Diagnostics of the two-way phase's sine and cosine, against double: the
+ * compensated form's (fn 9 sine, 10 cosine: the exact k r of range a[i] and
+ * wave number b[i], reduced by reduce_pio2_df, sincos_df's double-float
+ * values) and the plain form's
+ * (fn 11, 12: rsm_sincosf of the rounded k r).  out[i] = error. */
+__global__ void k_eval_phase(int fn, const float *a, const float *b, float *out, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float r = a[i], k = b[i];
+    double ref_s, ref_c;
+    sincos((double)k * (double)r, &ref_s, &ref_c);
+    double ss, cc;
+    if (fn == 9 || fn == 10) {
+        float phh, phl, q, rh, rl, sh, sl, ch, cl;
+        two_prod(k, r, phh, phl);
+        reduce_pio2_df(phh, phl, 0.0f, q, rh, rl);
+        sincos_df(rh, rl, q, sh, sl, ch, cl);
+        ss = (double)sh + (double)sl;
+        cc = (double)ch + (double)cl;
+    } else {
+        float s32, c32;
+        rsm_sincosf(k * r, &s32, &c32);
+        ss = s32;
+        cc = c32;
+    }
+    out[i] = (fn == 9 || fn == 11) ? (float)(ss - ref_s) : (float)(cc - ref_c);
+}
+
+/* The beam angle theta between b = sim[0..2] and p as a double-float, from
+ * s = |b x p| / (|b| |p|) (sh + sl) and the FP32 dot product: an FP32 first
+ * guess (asin(s) = s + s z P(z) below 30 degrees, atan2 beyond and behind
+ * the radar), then -- unless the antenna table clamps there anyway -- one
+ * Newton step with the guess's sine and cosine as double-floats
+ * (sincos_df): on sin theta = s where |cos theta| >= 0.7 (below 45 and
+ * above 135 degrees), where it is well conditioned, and on
+ * cos theta = b.p / (|b| |p|) (the dot product split exactly) between.
+ * The guess is good to ~1e-7 of theta, so the step leaves ~1e-15 rad, which
+ * the steep flanks of the antenna table's sidelobes need: an FP32 angle
+ * there moves a small weight by 1e-6 of itself. */
+__device__ __forceinline__ void beam_angle_df(const PulseArgs &P, float4 p, float sh, float sl, float dot, float cnh,
+                                              float dph, float dpl, float &ang_h, float &ang_l) {
+    const float *sd = P.sim;
+    float th0;
+    if (dot > 0.0f && sh < 0.5f) {
+        const float z = sh * sh;
+        th0 = fmaf(sh * z, rsm_asin_poly(z), sh);
+    } else {
+        th0 = rsm_atan2f(cnh, dot);
+    }
+    ang_h = th0;
+    ang_l = 0.0f;
+    const float fs = fmaf(th0, P.awd[0], P.awd[1]);
+    if (!(fs > -1.0f && fs < P.awd[2] + 1.0f)) return;   /* the table clamps: its edge entry */
+    float q = 0.0f, rh = th0, rl = 0.0f;
+    if (th0 > 0.78f) reduce_pio2_df(th0, 0.0f, 0.0f, q, rh, rl);
+    float s0h, s0l, c0h, c0l;
+    sincos_df(rh, rl, q, s0h, s0l, c0h, c0l);
+    float d;
+    if (fabsf(c0h) >= 0.7f) {
+        d = __fdividef((sh - s0h) + (sl - s0l), c0h);
+    } else {
+        /* c = b.p / (|b| |p|) as a double-float */
+        float a0, e0, a1, e1, a2, e2, th, tl;
+        two_prod(sd[0], p.x, a0, e0);
+        two_prod(sd[1], p.y, a1, e1);
+        two_prod(sd[2], p.z, a2, e2);
+        df_add(a0, e0, a1, e1, th, tl);
+        df_add(th, tl, a2, e2, th, tl);
+        float ch, cl;
+        df_div(th, tl, dph, dpl, ch, cl);
+        d = -__fdividef((ch - c0h) + (cl - c0l), s0h);
+    }
+    two_sum(th0, d, ang_h, ang_l);
+}
+
+/* compensated signal, every factor a double-float.  Range r = |p| from the
+ * exact squares of the FP32 position; the beam angle from
+ * |b x p| / (|b| |p|) with the cross product formed exactly, refined to a
+ * double-float by beam_angle_df; the antenna weight as
+ * the lerp of its table at that angle (weight_comp_df); the phase k r split
+ * exactly, reduced by pi/2 as a double-float (reduce_pio2_df) and its sine
+ * and cosine as double-floats (sincos_df); 1 / r^2 from the double-float
+ * r^2 with one Newton correction; the rotation a cc + b ss with both
+ * products split exactly.  The term (rotation x attenuation x antenna
+ * weight) leaves as head s and tail s_lo: the FP32 rounding of its factors,
+ * some 1e-7 of it each, is carried instead of dropped, so a gate sum of
+ * such terms reaches the FP64 pulse of the same state to the double-float's
+ * own precision. */
 __device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4 x, Sig32 &o) {
     const float *sd = P.sim;
     /* range */
@@ -162,45 +389,43 @@ __device__ __forceinline__ void signal_comp(const PulseArgs &P, float4 p, float4
     df_div(cnh, cnl, dph, dpl, sh, sl);
     const float dot = fmaf(bx, p.x, fmaf(by, p.y, bz * p.z));
     float ang_h, ang_l;
-    if (dot > 0.0f && sh < 0.5f) {
-        /* asin(s) = s + s z P(z): the P term is < 2% of s, float is enough */
-        const float z = sh * sh;
-        const float corr = rsm_asin_core(sh, z) - sh;
-        df_add(sh, sl, corr, 0.0f, ang_h, ang_l);
-    } else {
-        /* beyond 30 degrees (or behind the radar) the antenna table has
-         * clamped to its last entry long before */
-        ang_h = dot > 0.0f ? rsm_atan2f(cnh, dot) : RSC_PI_F;
-        ang_l = 0.0f;
-    }
-    o.wang = weight_comp(P.aw, P.awd, ang_h, ang_l);
-    /* phase */
-    float phh, phl;
+    beam_angle_df(P, p, sh, sl, dot, cnh, dph, dpl, ang_h, ang_l);
+    float wah, wal;
+    weight_comp_df(P.aw, P.awd, ang_h, ang_l, wah, wal);
+    o.wang = wah;
+    /* phase k r = k rh + k rl, both products split exactly: the head of
+     * k rh is reduced by pi/2 and the three small parts (up to 0.25 rad at
+     * 30 km) join after the reduction, where a double-float holds them to
+     * 1e-15 rad; then its sine and cosine */
+    float phh, phl, pa, pb, xsh, xse;
     two_prod(sd[4], rh, phh, phl);
-    phl = fmaf(sd[4], rl, phl);
-    float q;
-    float red = rsm_reduce_pio2(phh, &q);
-    red = red + phl;
-    float ss, cc;
-    rsm_sincos_reduced(red, q, &ss, &cc);
-    /* attenuation 1 / r^2 from the double-float r^2 */
-    const float inv = 1.0f / r2h;
-    const float atten = fmaf(-inv, r2l * inv, inv);
-    /* the rotation a cc + b ss with the product b ss exact (its rounding
-     * error folded back by an FMA), then one product by atten * wang */
-    const float k = atten * o.wang;
-    float rot[4];
+    two_prod(sd[4], rl, pa, pb);
+    two_sum(phl, pa, xsh, xse);
+    float q, red_h, red_l;
+    reduce_pio2_df(phh, xsh, xse + pb, q, red_h, red_l);
+    float ssh, ssl, cch, ccl;
+    sincos_df(red_h, red_l, q, ssh, ssl, cch, ccl);
+    /* attenuation 1 / r^2: y = 1 / r2h corrected by its residual */
+    const float y = 1.0f / r2h;
+    const float res = fmaf(-r2h, y, 1.0f) - r2l * y;
+    float ath, atl;
+    fast_two_sum(y, y * res, ath, atl);
+    /* k = attenuation x antenna weight */
+    float kh, kl;
+    df_mul_pair(ath, atl, wah, wal, kh, kl);
     const float xa[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
     for (int l = 0; l < 4; l++) {
-        const float a = xa[l], b = (l & 1) ? -xa[l - 1] : xa[l + 1];   /* (x.x, x.y) -> x.x cc + x.y ss, x.y cc - x.x ss */
-        const float p = b * ss;
-        const float pe = fmaf(b, ss, -p);
-        rot[l] = fmaf(a, cc, p) + pe;
+        /* (x.x, x.y) -> x.x cc + x.y ss, x.y cc - x.x ss */
+        const float a = xa[l], b = (l & 1) ? -xa[l - 1] : xa[l + 1];
+        float p1, e1, p2, e2, rot_h, e;
+        two_prod(a, cch, p1, e1);
+        two_prod(b, ssh, p2, e2);
+        two_sum(p1, p2, rot_h, e);
+        const float rot_l = e + fmaf(a, ccl, fmaf(b, ssl, e1 + e2));
+        o.sig[l] = rot_h * ath;
+        df_mul_pair(rot_h, rot_l, kh, kl, o.s.v[l], o.s_lo[l]);
     }
-#pragma unroll
-    for (int l = 0; l < 4; l++) o.sig[l] = rot[l] * atten;
-    o.s.set(rot[0] * k, rot[1] * k, rot[2] * k, rot[3] * k);
     o.r = rh;
     o.r_lo = rl;
 }
@@ -262,28 +487,44 @@ __device__ __forceinline__ void warp_reduce4_add(float *bin, unsigned lane, floa
  * accumulator, the last block converting (finish).  Used by the pulse kernel
  * (scatterers loaded from memory) and by the fused step kernel (scatterers
  * just advanced, in registers). */
-/* The same warp sum added into a double-float bin row (hi[0..3], lo[0..3])
- * with an error-free addition: the compensated form's coherent path, which
- * then needs no FP32 mini bins. */
-__device__ __forceinline__ void warp_reduce4_add_df(float *df, unsigned lane, float v0, float v1, float v2, float v3) {
+/* The warp's sum of four double-float values (heads v, tails u) added into
+ * a double-float bin row (hi[0..3], lo[0..3]): the transposed butterfly of
+ * warp_reduce4_add with an error-free addition of the heads at every level,
+ * their rounding errors joining the tails, which are summed alongside in
+ * FP32 (they are some 1e-7 of the heads: their own rounding is below
+ * 1e-14 of the sum).  The compensated form's path for a state in spatial
+ * order. */
+__device__ __forceinline__ void warp_reduce4_add_df(float *df, unsigned lane, const float *v, const float *u) {
     const bool h16 = (lane & 16u) != 0;
-    float k0 = h16 ? v2 : v0, k1 = h16 ? v3 : v1;
-    const float s0 = h16 ? v0 : v2, s1 = h16 ? v1 : v3;
-    k0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
-    k1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+    float k0 = h16 ? v[2] : v[0], k1 = h16 ? v[3] : v[1];
+    float t0 = h16 ? u[2] : u[0], t1 = h16 ? u[3] : u[1];
+    const float s0 = h16 ? v[0] : v[2], s1 = h16 ? v[1] : v[3];
+    const float z0 = h16 ? u[0] : u[2], z1 = h16 ? u[1] : u[3];
+    float a, e;
+    two_sum(k0, __shfl_xor_sync(0xffffffffu, s0, 16), a, e);
+    k0 = a;
+    t0 = t0 + (__shfl_xor_sync(0xffffffffu, z0, 16) + e);
+    two_sum(k1, __shfl_xor_sync(0xffffffffu, s1, 16), a, e);
+    k1 = a;
+    t1 = t1 + (__shfl_xor_sync(0xffffffffu, z1, 16) + e);
     const bool h8 = (lane & 8u) != 0;
-    float k = h8 ? k1 : k0;
-    const float s = h8 ? k0 : k1;
-    k = k + __shfl_xor_sync(0xffffffffu, s, 8);
-    k = k + __shfl_xor_sync(0xffffffffu, k, 4);
-    k = k + __shfl_xor_sync(0xffffffffu, k, 2);
-    k = k + __shfl_xor_sync(0xffffffffu, k, 1);
-    if ((lane & 7u) == 0u && k != 0.0f) {
+    float k = h8 ? k1 : k0, t = h8 ? t1 : t0;
+    const float s = h8 ? k0 : k1, z = h8 ? t0 : t1;
+    two_sum(k, __shfl_xor_sync(0xffffffffu, s, 8), a, e);
+    k = a;
+    t = t + (__shfl_xor_sync(0xffffffffu, z, 8) + e);
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) {
+        two_sum(k, __shfl_xor_sync(0xffffffffu, k, off), a, e);
+        k = a;
+        t = t + (__shfl_xor_sync(0xffffffffu, t, off) + e);
+    }
+    if ((lane & 7u) == 0u && (k != 0.0f || t != 0.0f)) {
         const unsigned c = lane >> 3;
-        float hi, e;
+        float hi;
         two_sum(df[c], k, hi, e);
         df[c] = hi;
-        df[4 + c] = df[4 + c] + e;
+        df[4 + c] = df[4 + c] + (e + t);
     }
 }
 
@@ -358,6 +599,7 @@ struct PulseBins {
                     signal_comp(P, p, x, sg);
                 }
                 c.set(sg.s.v[0], sg.s.v[1], sg.s.v[2], sg.s.v[3]);
+                if constexpr (MODE == 1) c.set_lo(sg.s_lo);
                 r = sg.r;
                 r_lo = sg.r_lo;
                 finite = fabsf(r) < INFINITY && finite4(sg.s.v);
@@ -404,18 +646,17 @@ struct PulseBins {
                 if (MODE == 0) rkj = __ldg(P.rk + w_lo);
                 for (int gate = w_lo; gate <= w_hi; gate++) {
                     float w = 0.0f;
-                    if (gate >= k_lo && gate <= k_hi) {
-                        if constexpr (MODE == 1) {
-                            w = range_weight_comp(P.rw, P.rwd, P.rw_tri, r - __ldg(P.rk + gate),
-                                                  r_lo - __ldg(P.rk_lo + gate));
-                        } else {
-                            w = range_weight_reg(P, r - rkj);
-                        }
-                    }
                     if constexpr (MODE == 1) {
-                        warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, w * c.v[0],
-                                            w * c.v[1], w * c.v[2], w * c.v[3]);
+                        float wl = 0.0f;
+                        if (gate >= k_lo && gate <= k_hi) {
+                            range_weight_comp_df(P.rw, P.rwd, P.rw_tri, r - __ldg(P.rk + gate),
+                                                 r_lo - __ldg(P.rk_lo + gate), w, wl);
+                        }
+                        Acc cw;
+                        c.scale_df(w, wl, cw);
+                        warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, cw.v, cw.u);
                     } else {
+                        if (gate >= k_lo && gate <= k_hi) w = range_weight_reg(P, r - rkj);
                         warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, w * c.v[0], w * c.v[1],
                                          w * c.v[2], w * c.v[3]);
                     }
@@ -439,10 +680,17 @@ struct PulseBins {
                         }
                         if (w != 0.0f) {
                             float *b = fbins + (size_t)gate * kBinStride32;
-                            atomicAdd(b + 0, w * c.v[0]);
-                            atomicAdd(b + 1, w * c.v[1]);
-                            atomicAdd(b + 2, w * c.v[2]);
-                            atomicAdd(b + 3, w * c.v[3]);
+                            float t[4] = {w * c.v[0], w * c.v[1], w * c.v[2], w * c.v[3]};
+                            if constexpr (MODE == 1) {
+                                /* unordered state: each term rounded once into
+                                 * the FP32 mini bins (its tail included first) */
+#pragma unroll
+                                for (int l = 0; l < 4; l++) t[l] = fmaf(w, c.v[l], w * c.u[l]);
+                            }
+                            atomicAdd(b + 0, t[0]);
+                            atomicAdd(b + 1, t[1]);
+                            atomicAdd(b + 2, t[2]);
+                            atomicAdd(b + 3, t[3]);
                         }
                     }
                     rkj = rkj + P.rdelta;
@@ -484,7 +732,9 @@ struct PulseBins {
                     if constexpr (MODE == 2) {
                         c.scale(lerp64(P.rw, P.rwd, r64 - P.rk64[k]), cw);
                     } else if constexpr (MODE == 1) {
-                        c.scale(weight_comp(P.rw, P.rwd, r - __ldg(P.rk + k), r_lo - __ldg(P.rk_lo + k)), cw);
+                        float wh, wl;
+                        weight_comp_df(P.rw, P.rwd, r - __ldg(P.rk + k), r_lo - __ldg(P.rk_lo + k), wh, wl);
+                        c.scale_df(wh, wl, cw);
                     } else {
                         c.scale(range_weight(P, r - __ldg(P.rk + k)), cw);
                     }
@@ -524,7 +774,7 @@ struct PulseBins {
     __device__ __forceinline__ void add_k(const PulseArgs &P, const bool *in, const unsigned long long *idx,
                                           const float4 *pp, const float4 *xx) {
         static_assert(MODE == 0 || MODE == 1, "the grouped form is the plain or compensated one");
-        float c[K][4], rr[K], rl[K];
+        float c[K][4], cu[K][4], rr[K], rl[K];
         int klo[K], khi[K];
         bool bad = false;
         unsigned lo = 0xffffffffu, hi = 0u;
@@ -558,6 +808,11 @@ struct PulseBins {
             c[q][1] = sg.s.v[1];
             c[q][2] = sg.s.v[2];
             c[q][3] = sg.s.v[3];
+            if constexpr (MODE == 1) {
+                if (!in[q]) sg.s_lo[0] = sg.s_lo[1] = sg.s_lo[2] = sg.s_lo[3] = 0.0f;
+#pragma unroll
+                for (int l = 0; l < 4; l++) cu[q][l] = sg.s_lo[l];
+            }
         }
         if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll
@@ -574,28 +829,51 @@ struct PulseBins {
                 rk_hi = __ldg(P.rk + gate);
                 rk_lo = __ldg(P.rk_lo + gate);
             }
-            float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f, v3 = 0.0f;
+            if constexpr (MODE == 1) {
+                /* the lane's K weighted terms of the gate as double-floats,
+                 * added error-free (heads) before the warp's reduction */
+                float vh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, vl[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-            for (int q = 0; q < K; q++) {
-                float w = 0.0f;
-                if (gate >= klo[q] && gate <= khi[q]) {
-                    if constexpr (MODE == 1) {
-                        w = range_weight_comp(P.rw, P.rwd, TRI == 1 ? 1 : P.rw_tri, rr[q] - rk_hi, rl[q] - rk_lo);
-                    } else if constexpr (TRI == 1) {
-                        w = range_weight_tri(P.rwd, rr[q] - rkj);
-                    } else {
-                        w = range_weight_reg(P, rr[q] - rkj);
+                for (int q = 0; q < K; q++) {
+                    float w = 0.0f, wl = 0.0f;
+                    if (gate >= klo[q] && gate <= khi[q]) {
+                        range_weight_comp_df(P.rw, P.rwd, TRI == 1 ? 1 : P.rw_tri, rr[q] - rk_hi, rl[q] - rk_lo, w,
+                                             wl);
+                    }
+#pragma unroll
+                    for (int l = 0; l < 4; l++) {
+                        float th, tl;
+                        df_mul_pair(c[q][l], cu[q][l], w, wl, th, tl);
+                        if (q == 0) {
+                            vh[l] = th;
+                            vl[l] = tl;
+                        } else {
+                            float a, e;
+                            two_sum(vh[l], th, a, e);
+                            vh[l] = a;
+                            vl[l] = vl[l] + (tl + e);
+                        }
                     }
                 }
-                /* fused: the lane's K terms of a gate in one rounding each */
-                v0 = fmaf(w, c[q][0], v0);
-                v1 = fmaf(w, c[q][1], v1);
-                v2 = fmaf(w, c[q][2], v2);
-                v3 = fmaf(w, c[q][3], v3);
-            }
-            if constexpr (MODE == 1) {
-                warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, v0, v1, v2, v3);
+                warp_reduce4_add_df(reinterpret_cast<float *>(wbins) + (size_t)gate * 8, lane, vh, vl);
             } else {
+                float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f, v3 = 0.0f;
+#pragma unroll
+                for (int q = 0; q < K; q++) {
+                    float w = 0.0f;
+                    if (gate >= klo[q] && gate <= khi[q]) {
+                        if constexpr (TRI == 1) {
+                            w = range_weight_tri(P.rwd, rr[q] - rkj);
+                        } else {
+                            w = range_weight_reg(P, rr[q] - rkj);
+                        }
+                    }
+                    /* fused: the lane's K terms of a gate in one rounding each */
+                    v0 = fmaf(w, c[q][0], v0);
+                    v1 = fmaf(w, c[q][1], v1);
+                    v2 = fmaf(w, c[q][2], v2);
+                    v3 = fmaf(w, c[q][3], v3);
+                }
                 warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, v0, v1, v2, v3);
             }
             rkj = rkj + P.rdelta;

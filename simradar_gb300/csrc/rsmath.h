@@ -246,14 +246,18 @@ RSM_FN float rsm_log1pf(float x) {
     return fk * RSM_LN2_HI + fmaf(fk, RSM_LN2_LO, rsm_log1p_core(m - 1.0f) + e * inv);
 }
 
-/* asin on |s| <= 1/2 : s + s z P(z), z = s^2, P the degree-4 fit */
-RSM_FN float rsm_asin_core(float s, float z) {
+/* the degree-4 fit P of asin(s) = s + s z P(z), z = s^2, |s| <= 1/2 */
+RSM_FN float rsm_asin_poly(float z) {
     float p = 0x1.5625d6p-5f;
     p = fmaf(p, z, 0x1.8ff98cp-6f);
     p = fmaf(p, z, 0x1.741a60p-5f);
     p = fmaf(p, z, 0x1.330612p-4f);
-    p = fmaf(p, z, 0x1.5555bap-3f);
-    return fmaf(s * z, p, s);
+    return fmaf(p, z, 0x1.5555bap-3f);
+}
+
+/* asin on |s| <= 1/2 : s + s z P(z) */
+RSM_FN float rsm_asin_core(float s, float z) {
+    return fmaf(s * z, rsm_asin_poly(z), s);
 }
 
 /* Every acos of the kernels takes a cosine formed from unit vectors or a unit

@@ -107,6 +107,7 @@ def load_library():
         "rsc_eval_math": ([I, _f32p, _f32p, _f32p, S], I),
         "rsc_autotune": ([P, _f32p, ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "rsc_set_pulse_shape": ([P, I, I], I),
+        "rsc_set_advance_shape": ([P, I], I),
         "rsc_set_sort_interval": ([P, I], I),
         "rsc_set_fused_step": ([P, I], I),
         "rsc_sort_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
@@ -114,6 +115,7 @@ def load_library():
         "rsc_batch_free": ([P], I),
         "rsc_batch_set_populations": ([P, ctypes.POINTER(Population)], I),
         "rsc_batch_set_precision": ([P, I], I),
+        "rsc_batch_set_persistent": ([P, I], I),
         "rsc_batch_autotune": ([P, _f32p], I),
         "rsc_batch_run": ([P, I, _f32p, ctypes.POINTER(ctypes.c_int32), _f32p, I], I),
         "rsc_batch_run_async": ([P, I, _f32p, ctypes.POINTER(ctypes.c_int32), _f32p, I], I),
@@ -370,6 +372,10 @@ class Worker:
         """Fix the pulse kernel's launch shape (0 = the largest that fits)."""
         _check(self._lib.rsc_set_pulse_shape(self._h, int(warps), int(blocks_per_sm)))
 
+    def set_advance_shape(self, scatterers_per_thread):
+        """Background scatterers per advance thread, 1 or 2 (rsc_set_advance_shape)."""
+        _check(self._lib.rsc_set_advance_shape(self._h, int(scatterers_per_thread)))
+
 
 class Batch:
     """Many workers stepped together: three launches per step for all of them
@@ -411,6 +417,10 @@ class Batch:
 
     def set_precision(self, mode):
         _check(self._lib.rsc_batch_set_precision(self._h, int(mode)))
+
+    def set_persistent(self, enable):
+        """Run every step of a run in one launch (rsc_batch_set_persistent)."""
+        _check(self._lib.rsc_batch_set_persistent(self._h, 1 if enable else 0))
 
     def autotune(self, sim_descs):
         d = f32(sim_descs).reshape(len(self.workers), 16)

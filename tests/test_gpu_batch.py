@@ -142,6 +142,48 @@ def test_batch_graph_equals_stream(backend, scenes):
         o.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_persistent_equals_graph(backend, oracle_lib, scenes, precision):
+    """The persistent form -- every step of a run in one launch -- against
+    the three-launch graph over runs of 3, 1 and 2 steps (odd runs leave the
+    state in the other pos / rcs pair): the state bit for bit, the pulses
+    within the summation bound, one launch per run; and the state after the
+    runs is the oracle's."""
+    O = oracle_lib
+    wa = _workers(backend, scenes, precision=precision)
+    wb = _workers(backend, scenes, precision=precision)
+    Ba, Bb = backend.Batch(wa), backend.Batch(wb)
+    pops = [synth.population(S) for S in scenes]
+    Ba.set_populations(pops)
+    Bb.set_populations(pops)
+    Ba.set_precision(precision)
+    Bb.set_precision(precision)
+    Bb.set_persistent(True)
+    sts = [O.OracleState(S.state) for S in scenes]
+    k0 = 0
+    for run in (3, 1, 2):
+        sims, les = _steps(scenes, k0, run)
+        n0 = Bb.launch_count
+        pa = Ba.run(sims, les, use_graph=True)
+        pb = Bb.run(sims, les)
+        assert Bb.launch_count - n0 == 1
+        scale = np.abs(pa).max(axis=(2, 3), keepdims=True) + 1e-30
+        assert np.all(np.isfinite(pb))
+        assert np.all(np.abs(pa - pb) <= 1e-4 * scale), np.abs(pa - pb).max()
+        for j in range(run):
+            for i, S in enumerate(scenes):
+                O.advance_time(sts[i], S, S.counts, S.les[0], sims[j, i])
+        for x, y in zip(wa, wb):
+            sa, sb = x.download(STATE_FIELDS), y.download(STATE_FIELDS)
+            for f in STATE_FIELDS:
+                assert np.array_equal(bits(sa[f]), bits(sb[f])), (f, k0)
+        k0 += run
+    for i, W in enumerate(wb):
+        assert_state_equal(W.download(STATE_FIELDS), sts[i].s, where="instance %d " % i)
+    for o in [Ba, Bb] + wa + wb:
+        o.close()
+
+
 def test_batch_autotune_and_compensated(backend, oracle_lib, scenes):
     """The autotuner picks a reachable shape and leaves the state alone; the
     compensated form in a batch keeps its bound against FP64."""

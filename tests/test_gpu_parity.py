@@ -136,6 +136,29 @@ def test_triangle_weight_matches_table_lerp(backend, oracle_lib):
         int((bits(g) != bits(c)).sum()), a.size)
 
 
+def test_compensated_phase_sine_cosine(backend):
+    """The compensated pulse's sine and cosine of the two-way phase k r
+    (reduce_pio2_df + sincos_df, as double-floats) against double, for
+    ranges near the radar and 30 km out (phases to 4.2e6 rad), and for
+    ranges placed on multiples of pi/2 / k and of 1/128 rad past them (the
+    reduction's and the table's nodes and midpoints): within 1e-13.  The
+    plain FP32 form, for scale, is off by up to a quarter at 30 km."""
+    rng = np.random.default_rng(17)
+    k = np.float32(4.0 * np.pi / 0.1)
+    r = [rng.uniform(1.0, 50.0, 50000), rng.uniform(1800.0, 2500.0, 100000),
+         rng.uniform(31000.0, 33000.0, 100000)]
+    n = np.arange(1, 2600000, 997, dtype=np.float64)
+    r.append(n * (np.pi / 2) / float(k))
+    r.append((n * (np.pi / 2) + (np.arange(n.size) % 205 - 102) / 128.0) / float(k))
+    a = np.concatenate(r).astype(np.float32)
+    b = np.full_like(a, k)
+    for fn in (9, 10):
+        e = np.abs(backend.eval_math(fn, a, b).astype(np.float64))
+        assert e.max() <= 1.0e-13, "fn %d: %.3g at r = %r" % (fn, e.max(), a[np.argmax(e)])
+    far = a > 30000.0
+    assert np.abs(backend.eval_math(11, a[far], b[far])).max() > 0.05
+
+
 def test_advance_dbu_bitexact(backend, oracle_lib, scene_db):
     """Concept DBU (el_atts, bounded) rain + three debris types, 6 steps."""
     W, st, _ = run_pair(backend, oracle_lib, scene_db, 6)
@@ -181,35 +204,40 @@ def test_pulse_f64_matches_cpu_f64(backend, oracle_lib, scene_db):
     W.close()
 
 
-# Compensated form against FP64: |gpu - fp64| <= COMP_REL * |gate| (the gate's
-# complex magnitude per polarization), except where the gate's terms cancel
-# or are all tiny.  Each term w_i x_i is formed in FP32 from FP32 inputs
-# (table lerps, 1/r^2, sin/cos of the split phase, the rotation and two
-# products): about 1e-7 of |w_i x_i| typically, but a lerp between table
-# entries of different size (far antenna sidelobes) or a weight near the
-# edge of its support carries an error set by the larger entry, up to a few
-# 1e-6 of the small result; the sum itself adds almost nothing.  With
-# kappa = sum|x| / |sum x| the bound is max(COMP_REL |gate|, COMP_ABS sum|x|),
-# and gates with kappa <= 10 must meet COMP_REL outright.
+# Compensated form against FP64: every factor of every term is a
+# double-float and the sums are error-free, so the pulse reaches the FP64
+# pulse of the same state to the FP32 rounding of its output (6e-8 of a
+# component) plus the double-float's own precision (the range to 2^-48, a
+# phase error of ~1e-8 rad at 30 km, which shows only where a gate's terms
+# cancel by 1e4 or more).  Asserted per gate and lane, raw (every gate with
+# a non-zero FP64 value, whatever its terms do): |gpu - fp64| <= COMP_REL
+# |gate| (the gate's complex magnitude per polarization), and <= COMP_TIGHT
+# |gate| on gates whose terms cancel by less than 100x.
 COMP_REL = 1.0e-5
-COMP_ABS = 5.0e-6
+COMP_TIGHT = 2.0e-7
 
 
 def assert_comp_close(g, r64, ab, what=""):
     mag = np.hypot(r64[:, 0::2], r64[:, 1::2]).repeat(2, axis=1)
     err = np.abs(g.astype(np.float64) - r64)
-    lim = np.maximum(COMP_REL * mag, COMP_ABS * ab) + 1e-30
-    bad = np.argwhere(err > lim)
-    assert bad.size == 0, "%s: %d values beyond the compensated bound; first (gate, lane) %s err %r |gate| %r sum|x| %r" % (
-        what, len(bad), tuple(bad[0]), err[tuple(bad[0])], mag[tuple(bad[0])], ab[tuple(bad[0])])
-    well = (ab <= 10.0 * mag) & (mag > 0)
+    zero = mag == 0
+    assert np.all(err[zero] == 0.0), "%s: non-zero output on a gate with no contribution" % what
+    nz = ~zero
+    rel = err[nz] / mag[nz]
+    if rel.size:
+        k = np.argmax(rel)
+        where = tuple(np.argwhere(nz)[k])
+        assert rel[k] <= COMP_REL, "%s: relative error %.3g at (gate, lane) %s, |gate| %r sum|x| %r" % (
+            what, rel[k], where, mag[where], ab[where])
+    well = nz & (ab <= 100.0 * mag)
     if well.any():
-        assert (err[well] / mag[well]).max() <= COMP_REL, what
+        assert (err[well] / mag[well]).max() <= COMP_TIGHT, "%s: %.3g on a well-conditioned gate" % (
+            what, (err[well] / mag[well]).max())
 
 
 def test_pulse_compensated_error(backend, oracle_lib, scene_db):
     """Compensated form: per-gate relative I/Q error <= 1e-5 against FP64 on
-    gates with kappa <= 10, and within COMP_ABS sum|x| elsewhere."""
+    every gate, <= 2e-7 where the terms cancel by less than 100x."""
     W, st, pulses = run_pair(backend, oracle_lib, scene_db, 3, precision=1, check_each=False)
     for k, (g, r, r64, ab) in enumerate(pulses):
         assert_comp_close(g, r64, ab, "pulse %d" % k)
