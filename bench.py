@@ -579,7 +579,7 @@ def bench_large(torch, rsc, synth, dev, chunks, chunk=100):
             "iq_nonzero_pulses": int((np.abs(iq).sum(axis=(1, 2)) > 0).sum())}
 
 
-def bench_les(torch, rsc, synth, dev, S, steps=400, period=100):
+def bench_les(torch, rsc, synth, dev, S, steps=2000, period=100, repeats=3):
     """The LES frame swap inside the pulse loop (rs.c:5188-5200): every
     `period` steps the next frame goes into the inactive slot and the loop
     moves to it.  Three ways on the README workload: no swap; the reference's
@@ -628,16 +628,26 @@ def bench_les(torch, rsc, synth, dev, S, steps=400, period=100):
     # the reference's frames arrive remapped by les.c's background thread
     host_frames = [src.read(f)[:2] for f in range(frames)]
     loop("source")   # page the frames in, pin the source's buffers
-    none_ms, _ = loop("none")
-    ref_ms, ref_call = loop("blocking")
-    src_ms, src_call = loop("source")
+    # the three loops interleaved, each run `repeats` times: the median of
+    # each (the loop is timed on the host clock, which a busy host jolts)
+    runs = {"none": [], "blocking": [], "source": []}
+    for _ in range(repeats):
+        for mode in ("none", "blocking", "source"):
+            runs[mode].append(loop(mode))
+    none_ms = statistics.median(r[0] for r in runs["none"])
+    ref_ms = statistics.median(r[0] for r in runs["blocking"])
+    ref_call = statistics.median(r[1] for r in runs["blocking"])
+    src_ms = statistics.median(r[0] for r in runs["source"])
+    src_call = statistics.median(r[1] for r in runs["source"])
     W.close()
     src.close()
     shutil.rmtree(tmpdir, ignore_errors=True)
     nn = S.les_cfg.nx * S.les_cfg.ny * S.les_cfg.nz
     swaps = steps // period
-    return {"workload": "README loop (2M scatterers), LES %dx%dx%d, a frame swap every %d steps, %d steps"
-                        % (S.les_cfg.nx, S.les_cfg.ny, S.les_cfg.nz, period, steps),
+    return {"workload": "README loop (2M scatterers), LES %dx%dx%d, a frame swap every %d steps, %d steps, "
+                        "each way run %d times interleaved (medians)"
+                        % (S.les_cfg.nx, S.les_cfg.ny, S.les_cfg.nz, period, steps, repeats),
+            "runs_ms_per_step": {k: [r[0] for r in v] for k, v in runs.items()},
             "ms_per_step_no_swap": none_ms,
             "ms_per_step_blocking_swap": ref_ms, "blocking_swap_call_ms": ref_call,
             "ms_per_step_source_swap": src_ms, "source_swap_call_ms": src_call,

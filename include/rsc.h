@@ -175,6 +175,14 @@ int rsc_set_pulse_precision(rsc_worker *w, int mode);
  * them on download.  Default 0. */
 int rsc_set_materialize_sig_aux(rsc_worker *w, int enable);
 
+/* The compensated form's gate sums on the triangle range weight (additive,
+ * default 1): 1 sums each scatterer's term into its one range interval as
+ * two moments (the triangle is linear within an interval) and forms the
+ * gates from them; 0 weighs every term into every gate it reaches.  Both
+ * are error-free double-float sums; the pulses agree to the double-float's
+ * precision.  Read by rsc_make_pulse and by a batch's runs. */
+int rsc_set_pulse_moments(rsc_worker *w, int enable);
+
 /* Number of kernel launches this worker has issued (for accounting). */
 int rsc_launch_count(rsc_worker *w, uint64_t *count);
 

@@ -122,6 +122,7 @@ struct rsc_worker {
     /* modes and bookkeeping */
     int precision = RSC_PULSE_PLAIN;
     int materialize = 0;
+    int moments = 1;          /* rsc_set_pulse_moments */
     bool sig_aux_stale = false;
     bool have_pulse_desc = false;
     /* the pos / rcs pair the latest pulse read: its aux / sig, when the pulse
@@ -482,10 +483,19 @@ int pulse_shape(int mode, bool batch, uint32_t G, int want_warps, int want_per_s
     cudaError_t e;
     if (!batch) {
         e = kernel_occupancy(pulse_kernel(mode, path), *threads, *smem, &per_sm);
-    } else if (mode == RSC_PULSE_PLAIN) {
-        e = kernel_occupancy(rsc::k_pulse_batch<0>, *threads, *smem, &per_sm);
-    } else if (mode == RSC_PULSE_COMPENSATED) {
-        e = kernel_occupancy(rsc::k_pulse_batch<1>, *threads, *smem, &per_sm);
+    } else if (mode == RSC_PULSE_PLAIN || mode == RSC_PULSE_COMPENSATED) {
+        /* both forms of the batched kernel (range table tested per gate, and
+         * the triangle compiled in) get the shared-memory limit raised; the
+         * shape is the one both fit */
+        int per_sm_tri = 1;
+        if (mode == RSC_PULSE_PLAIN) {
+            e = kernel_occupancy(rsc::k_pulse_batch<0>, *threads, *smem, &per_sm);
+            if (e == cudaSuccess) e = kernel_occupancy(rsc::k_pulse_batch<0, 1>, *threads, *smem, &per_sm_tri);
+        } else {
+            e = kernel_occupancy(rsc::k_pulse_batch<1>, *threads, *smem, &per_sm);
+            if (e == cudaSuccess) e = kernel_occupancy(rsc::k_pulse_batch<1, 1>, *threads, *smem, &per_sm_tri);
+        }
+        if (per_sm_tri < per_sm) per_sm = per_sm_tri;
     } else {
         e = kernel_occupancy(rsc::k_pulse_batch<2>, *threads, *smem, &per_sm);
     }
@@ -569,6 +579,17 @@ cudaError_t launch_advance(rsc_worker *w, const AdvanceArgs &a, unsigned blocks,
 
 void launch_pulse(int mode, const PulseArgs &P, int grid, int threads, size_t smem, cudaStream_t st) {
     pulse_kernel(mode, pulse_path(P, mode))<<<grid, threads, smem, st>>>(P);
+}
+
+/* The compensated form's interval moments (PulseArgs::mom_n): on the
+ * triangle range table whose support, 1 / scale, is a whole number of gate
+ * spacings (up to rsc::kMomMaxN), taken by the grouped pulse path. */
+int moment_span(const PulseArgs &P) {
+    if (!P.rw_tri || P.dense || !(P.rdelta > 0.0f) || !(P.rwd[0] > 0.0f)) return 0;
+    const double x = 1.0 / ((double)P.rwd[0] * (double)P.rdelta);
+    const double n = floor(x + 0.5);
+    if (n < 1.0 || n > (double)rsc::kMomMaxN || fabs(x - n) > 1.0e-6 * n) return 0;
+    return (int)n;
 }
 
 void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
@@ -1543,6 +1564,7 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
         P.rk = w->rk_hi;
         /* the error-free warp sums need the grouped path, whatever the order */
         P.coherent_span = (int)w->G + 1;
+        P.mom_n = w->moments ? moment_span(P) : 0;
     }
     const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
     P.materialize = mat ? 1 : 0;
@@ -1558,6 +1580,7 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
         size_t ssmem = 0;
         s = step_shape(mode, w, &sgrid, &ssmem);
         if (s) return s;
+        P.mom_n = 0;   /* the fused kernel sums per gate */
         if (mode == RSC_PULSE_PLAIN) {
             rsc::k_step<0><<<sgrid, rsc::kAdvanceThreads, ssmem, w->stream>>>(w->pend_a, P, w->pend_blocks);
         } else {
@@ -1647,6 +1670,13 @@ int rsc_set_materialize_sig_aux(rsc_worker *w, int enable) {
     int s = check_worker(w);
     if (s) return s;
     w->materialize = enable ? 1 : 0;
+    return RSC_OK;
+}
+
+int rsc_set_pulse_moments(rsc_worker *w, int enable) {
+    int s = check_worker(w);
+    if (s) return s;
+    w->moments = enable ? 1 : 0;
     return RSC_OK;
 }
 
@@ -1841,6 +1871,7 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
         if (b->mode == RSC_PULSE_COMPENSATED) {
             P.rk = x->rk_hi;
             P.coherent_span = (int)x->G + 1;
+            P.mom_n = x->moments ? moment_span(P) : 0;
         }
         P.materialize = 0;
         tri = tri && P.rw_tri;
@@ -2086,6 +2117,7 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
     if (mode == RSC_PULSE_COMPENSATED) {
         P.rk = w->rk_hi;
         P.coherent_span = (int)w->G + 1;
+        P.mom_n = w->moments ? moment_span(P) : 0;
     }
     P.materialize = 0;
     s = pulse_d2h_wait(w);

@@ -475,6 +475,8 @@ struct PulseArgs {
     int dense;
     int coherent_span;   /* warp-coherent gate path when a warp spans fewer gates */
     int materialize;
+    int mom_n;           /* compensated form on the triangle whose support is mom_n gate spacings: terms
+                          * summed per range interval as moments (PulseBins::add_k), 0 otherwise */
     double *acc64;       /* G * 4 FP64 accumulators, zero between launches */
     unsigned *counter;
     float4 *pulse;

@@ -436,10 +436,25 @@ template <> struct PulseTraits<0> { typedef AccF32 Acc; static constexpr unsigne
 template <> struct PulseTraits<1> { typedef AccDF Acc; static constexpr unsigned kMain = 8; };
 template <> struct PulseTraits<2> { typedef AccF64 Acc; static constexpr unsigned kMain = 4; };
 
-/* shared memory per warp of k_pulse<MODE>, in bytes, for G gates */
+/* The block's flags (bit l for lane l) that a non-finite value met the
+ * moment form: that lane of every gate of the pulse is then NaN, as
+ * 0 x NaN is in pass 1. */
+__device__ __forceinline__ int &pulse_poison() {
+    __shared__ int flag;
+    return flag;
+}
+
+/* Largest triangle support, in gate spacings, of the compensated form's
+ * interval moments (PulseArgs::mom_n). */
+constexpr int kMomMaxN = 4;
+
+/* shared memory per warp of k_pulse<MODE>, in bytes, for G gates (the
+ * compensated form: double-float bins of G gates, or of G + 2 kMomMaxN - 1
+ * range intervals with two moments each, and FP32 mini bins) */
 __host__ __device__ constexpr size_t pulse_warp_bytes(int mode, unsigned G) {
     return mode == 0 ? (size_t)G * kBinStride32 * 4
-                     : (mode == 1 ? (size_t)G * (32 + kBinStride32 * 4) : (size_t)G * 32);
+                     : (mode == 1 ? (size_t)(G + 2 * kMomMaxN - 1) * 64 + (size_t)G * kBinStride32 * 4
+                                  : (size_t)G * 32);
 }
 
 /* block blk of the nblk blocks that form one pulse */
@@ -543,11 +558,16 @@ struct PulseBins {
     bin_t *bins, *wbins;
     float *mini, *fbins;
     unsigned G, words, nwarps, warp, lane;
+    int mom;
 
     __device__ __forceinline__ void init(const PulseArgs &P) {
         extern __shared__ __align__(16) unsigned char smem_raw[];
         G = P.G;
-        words = G * kMain;
+        mom = (MODE == 1) ? P.mom_n : 0;
+        /* interval moments: rows of 16 floats (S0 hi, lo, S1 hi, lo) for the
+         * intervals -mom .. G + mom - 2 */
+        words = mom ? (G + 2 * mom - 1) * 16 : G * kMain;
+        if (threadIdx.x == 0) pulse_poison() = 0;
         nwarps = blockDim.x >> 5;
         warp = threadIdx.x >> 5;
         lane = threadIdx.x & 31u;
@@ -761,6 +781,88 @@ struct PulseBins {
         }
     }
 
+    /* The compensated form's terms on the triangle whose support is mom
+     * gate spacings: within the range interval [rho_j, rho_j+1) between two
+     * gate origins every gate's weight is linear in r, 1 - |j - k| delta s
+     * -+ s u with u = r - rho_j (the sign by the side of gate k, s the
+     * table's scale), so a scatterer adds its term x to S0_j and u x to S1_j
+     * of its one interval, and finish forms each gate from the 2 mom
+     * intervals of its support.  A warp of sorted neighbours meets one or
+     * two intervals instead of the 4-5 gates their triangles reach, each
+     * with two error-free reductions.  rho_j = r_0 + j delta as a
+     * double-float; j from FP32, which can put a scatterer within 1e-4 m of
+     * an origin on the other side of it (its weight then off by 1e-5 of
+     * itself, for 1 in 1e5 scatterers). */
+    template <int K>
+    __device__ __forceinline__ void add_moments(const PulseArgs &P, const bool *in, const float *rr, const float *rl,
+                                                const float (*c)[4], const float (*cu)[4]) {
+        const int n = mom;
+        const float r0h = __ldg(P.rk), r0l = __ldg(P.rk_lo);
+        int bq[K];
+        float uh[K], ul[K];
+        unsigned lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            bq[q] = -1;
+            uh[q] = 0.0f;
+            ul[q] = 0.0f;
+            if (in[q]) {
+                const float jf = floorf((rr[q] - r0h) * P.inv_delta);
+                if (jf >= (float)(-n - 1) && jf <= (float)((int)G + n - 1)) {
+                    int j = (int)jf;
+                    float ph, pl, rho_h, rho_l;
+                    two_prod((float)j, P.rdelta, ph, pl);
+                    df_add(r0h, r0l, ph, pl, rho_h, rho_l);
+                    float u0 = rr[q] - rho_h, u1 = rl[q] - rho_l;
+                    /* j from the head in FP32 can be one off within 1e-3 m of
+                     * an origin (the range's tail is up to that): the
+                     * double-float offset puts the scatterer on its side */
+                    const float ut = u0 + u1;
+                    if (ut < 0.0f || ut >= P.rdelta) {
+                        const float sh = ut < 0.0f ? P.rdelta : -P.rdelta;
+                        float a, e;
+                        two_sum(u0, sh, a, e);
+                        u0 = a;
+                        u1 = u1 + e;
+                        j += ut < 0.0f ? -1 : 1;
+                    }
+                    if (j >= -n && j <= (int)G + n - 2) {
+                        uh[q] = u0;
+                        ul[q] = u1;
+                        bq[q] = j + n;
+                        lo = min(lo, (unsigned)bq[q]);
+                        hi = max(hi, (unsigned)bq[q]);
+                    }
+                }
+            }
+        }
+        const unsigned b_lo = __reduce_min_sync(0xffffffffu, lo);
+        const unsigned b_hi = __reduce_max_sync(0xffffffffu, hi);
+        if (b_lo == 0xffffffffu) return;   /* no lane's scatterer reaches a gate */
+        float *rows = reinterpret_cast<float *>(wbins);
+        for (unsigned b = b_lo; b <= b_hi; b++) {
+            /* S0 then S1 (fewer live registers than both at once) */
+#pragma unroll
+            for (int m = 0; m < 2; m++) {
+                float sh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sl[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+                for (int q = 0; q < K; q++) {
+                    if (bq[q] == (int)b) {
+#pragma unroll
+                        for (int l = 0; l < 4; l++) {
+                            float th = c[q][l], tl = cu[q][l], a, e;
+                            if (m == 1) df_mul_pair(c[q][l], cu[q][l], uh[q], ul[q], th, tl);
+                            two_sum(sh[l], th, a, e);
+                            sh[l] = a;
+                            sl[l] = sl[l] + (tl + e);
+                        }
+                    }
+                }
+                warp_reduce4_add_df(rows + (size_t)b * 16 + 8 * m, lane, sh, sl);
+            }
+        }
+    }
+
     /* K scatterers per lane (plain or compensated form, state in spatial
      * order): lane l
      * holds scatterers l, l + 32, ... of a run of 32 K neighbours, the warp
@@ -812,6 +914,39 @@ struct PulseBins {
                 if (!in[q]) sg.s_lo[0] = sg.s_lo[1] = sg.s_lo[2] = sg.s_lo[3] = 0.0f;
 #pragma unroll
                 for (int l = 0; l < 4; l++) cu[q][l] = sg.s_lo[l];
+            }
+        }
+        if constexpr (MODE == 1) {
+            if (mom) {
+                /* a non-finite value reaches its lane of every gate (0 x NaN
+                 * in pass 1): its lane is flagged NaN for the pulse and the
+                 * finite lanes are summed; a non-finite range flags all four */
+                bool use[K];
+#pragma unroll
+                for (int q = 0; q < K; q++) use[q] = in[q];
+                if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+                    for (int q = 0; q < K; q++) {
+                        if (!in[q]) continue;
+                        unsigned bits = 0u;
+                        if (!(fabsf(rr[q]) < INFINITY)) {
+                            bits = 15u;
+                            use[q] = false;
+                        } else {
+#pragma unroll
+                            for (int l = 0; l < 4; l++) {
+                                if (!(fabsf(c[q][l]) < INFINITY) || !(fabsf(cu[q][l]) < INFINITY)) {
+                                    bits |= 1u << l;
+                                    c[q][l] = 0.0f;
+                                    cu[q][l] = 0.0f;
+                                }
+                            }
+                        }
+                        if (bits) atomicOr(&pulse_poison(), (int)bits);
+                    }
+                }
+                add_moments<K>(P, use, rr, rl, c, cu);
+                return;
             }
         }
         if (__any_sync(0xffffffffu, bad)) {
@@ -880,8 +1015,57 @@ struct PulseBins {
         }
     }
 
+    /* The moment form's block sums: each interval's moments summed over
+     * the warps (into warp 0's rows), then gate k of lane l from the
+     * intervals j = k - mom .. k + mom - 1 of its support,
+     * sum (1 - |j - k| delta s) S0_j -+ s S1_j, as a double-float. */
+    __device__ __forceinline__ double moment_gate(const PulseArgs &P, unsigned k, unsigned l) const {
+        const float *all = reinterpret_cast<const float *>(bins);
+        const float sf = P.rwd[0];
+        float dsh, dsl;
+        two_prod(P.rdelta, sf, dsh, dsl);
+        float gh = 0.0f, gl = 0.0f;
+        for (int j = (int)k - mom; j <= (int)k + mom - 1; j++) {
+            const float *row = all + (size_t)(j + mom) * 16;
+            const int m = j >= (int)k ? j - (int)k : (int)k - j;
+            float mh, ml, ah, ae, t0h, t0l, t1h, t1l, x, e;
+            two_prod((float)m, dsh, mh, ml);
+            ml = fmaf((float)m, dsl, ml);
+            two_sum(1.0f, -mh, ah, ae);
+            df_mul_pair(ah, ae - ml, row[l], row[4 + l], t0h, t0l);
+            const float sg = j >= (int)k ? -sf : sf;
+            two_prod(sg, row[8 + l], t1h, t1l);
+            t1l = fmaf(sg, row[12 + l], t1l);
+            two_sum(gh, t0h, x, e);
+            gh = x;
+            gl = gl + (t0l + e);
+            two_sum(gh, t1h, x, e);
+            gh = x;
+            gl = gl + (t1l + e);
+        }
+        return (double)gh + (double)gl;
+    }
+
     __device__ __forceinline__ void finish(const PulseArgs &P, unsigned nblk) {
         __syncthreads();
+        if (MODE == 1 && mom) {
+            float *all = reinterpret_cast<float *>(bins);
+            const unsigned rows = (G + 2 * mom - 1) * 8;
+            for (unsigned o = threadIdx.x; o < rows; o += blockDim.x) {
+                const unsigned off = (o >> 3) * 16 + ((o >> 2) & 1u) * 8, l = o & 3u;
+                float hi = 0.0f, lo = 0.0f;
+                for (unsigned wv = 0; wv < nwarps; wv++) {
+                    const float *b = all + (size_t)wv * words + off;
+                    float x, e;
+                    two_sum(hi, b[l], x, e);
+                    hi = x;
+                    lo = lo + (e + b[4 + l]);
+                }
+                all[off + l] = hi;
+                all[off + 4 + l] = lo;
+            }
+            __syncthreads();
+        }
         /* block sum of each output (warp bins in warp order), added into the
          * grid's FP64 accumulator with one global atomic per output: no block
          * waits on another, and FP64 carries the FP32 and double-float block sums
@@ -890,7 +1074,9 @@ struct PulseBins {
         for (unsigned o = threadIdx.x; o < outs; o += blockDim.x) {
             const unsigned k = o >> 2, l = o & 3u;
             double v;
-            if constexpr (Acc::kWords == 2) {
+            if (MODE == 1 && mom) {
+                v = ((pulse_poison() >> l) & 1) ? (double)NAN : moment_gate(P, k, l);
+            } else if constexpr (Acc::kWords == 2) {
                 float hi = 0.0f, lo = 0.0f;
                 for (unsigned wv = 0; wv < nwarps; wv++) {
                     const float *b = reinterpret_cast<const float *>(bins) + (size_t)wv * words + k * 8;

@@ -101,6 +101,7 @@ def load_library():
         "rsc_download_pulse_async": ([P, P], I),
         "rsc_set_pulse_precision": ([P, I], I),
         "rsc_set_materialize_sig_aux": ([P, I], I),
+        "rsc_set_pulse_moments": ([P, I], I),
         "rsc_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
         "rsc_get_stream": ([P, ctypes.POINTER(P)], I),
         "rsc_get_advance_stream": ([P, ctypes.POINTER(P)], I),
@@ -326,6 +327,10 @@ class Worker:
 
     def set_materialize(self, enable):
         _check(self._lib.rsc_set_materialize_sig_aux(self._h, 1 if enable else 0))
+
+    def set_moments(self, enable):
+        """The compensated form's interval moments on or off (rsc_set_pulse_moments)."""
+        _check(self._lib.rsc_set_pulse_moments(self._h, 1 if enable else 0))
 
     @property
     def launch_count(self):

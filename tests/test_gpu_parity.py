@@ -244,6 +244,35 @@ def test_pulse_compensated_error(backend, oracle_lib, scene_db):
     W.close()
 
 
+def test_compensated_moments_and_per_gate(backend, oracle_lib, scene_db):
+    """The compensated form's two ways of summing on the triangle -- each
+    term into its range interval as two moments, or weighed into every gate
+    it reaches -- both within the bound against FP64, and the same pulse
+    within one FP32 rounding of its components, in the caller's order (the
+    first pulse) and in spatial order."""
+    O = oracle_lib
+    S = scene_db
+    pop = synth.population(S)
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    W.set_precision(1)
+    st = O.OracleState(S.state)
+    for k in range(3):
+        sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+        r64, ab = O.make_pulse_f64(st, S, sd, return_abs=True)
+        got = {}
+        for mom in (1, 0):
+            W.set_moments(mom)
+            W.make_pulse(sd)
+            got[mom] = W.download_pulse(1.0)
+            assert_comp_close(got[mom], r64, ab, "pulse %d moments %d" % (k, mom))
+        a, b = got[1].astype(np.float64), got[0].astype(np.float64)
+        assert np.all(np.abs(a - b) <= 1.2e-7 * np.maximum(np.abs(a), np.abs(b))), "pulse %d" % k
+        W.advance_time(pop, 0, sd)
+        O.advance_time(st, S, S.counts, S.les[0], sd)
+    W.close()
+
+
 def test_dense_gate_path(backend, oracle_lib):
     """A range weight with non-zero edges reaches every gate (dense path)."""
     S = synth.make_scene(num_rain=5000, les_count=1)
