@@ -315,7 +315,8 @@ __global__ void k_eval_phase(int fn, const float *a, const float *b, float *out,
  * cos theta = b.p / (|b| |p|) (the dot product split exactly) between.
  * The guess is good to ~1e-7 of theta, so the step leaves ~1e-15 rad, which
  * the steep flanks of the antenna table's sidelobes need: an FP32 angle
- * there moves a small weight by 1e-6 of itself. */
+ * there moves a small weight by 1e-6 of itself.  Below 5.7 degrees the
+ * asin series in double-float does the same for a fraction of the cost. */
 __device__ __forceinline__ void beam_angle_df(const PulseArgs &P, float4 p, float sh, float sl, float dot, float cnh,
                                               float dph, float dpl, float &ang_h, float &ang_l) {
     const float *sd = P.sim;
@@ -330,6 +331,26 @@ __device__ __forceinline__ void beam_angle_df(const PulseArgs &P, float4 p, floa
     ang_l = 0.0f;
     const float fs = fmaf(th0, P.awd[0], P.awd[1]);
     if (!(fs > -1.0f && fs < P.awd[2] + 1.0f)) return;   /* the table clamps: its edge entry */
+    if (dot > 0.0f && sh < 0.1f) {
+        /* below 5.7 degrees the series converges fast: asin s = s + s^3/6 +
+         * s^5 Q(s^2), Q the next Taylor terms (3/40, 15/336, 105/3456,
+         * 945/42240; the rest below 1e-9 of Q), with s^3/6 a double-float
+         * and s^5 Q below 8e-7 of s in FP32: within 1e-14 rad */
+        float zh, zl, ch3, cl3;
+        two_prod(sh, sh, zh, zl);
+        zl = fmaf(2.0f * sh, sl, zl);
+        df_mul_pair(sh, sl, zh, zl, ch3, cl3);                              /* s^3 */
+        float th, tl;
+        df_mul_pair(ch3, cl3, 0x1.555556p-3f, -0x1.555556p-28f, th, tl);  /* / 6 */
+        float q = fmaf(zh, 0x1.6e8ba2p-6f, 0x1.f1c71cp-6f);
+        q = fmaf(zh, q, 0x1.6db6dcp-5f);
+        q = fmaf(zh, q, 0x1.333334p-4f);
+        const float t5 = (ch3 * zh) * q;
+        float a, e;
+        two_sum(sh, th, a, e);
+        fast_two_sum(a, e + (sl + tl + t5), ang_h, ang_l);
+        return;
+    }
     float q = 0.0f, rh = th0, rl = 0.0f;
     if (th0 > 0.78f) reduce_pio2_df(th0, 0.0f, 0.0f, q, rh, rl);
     float s0h, s0l, c0h, c0l;
