@@ -382,6 +382,7 @@ def bench_batch(torch, rsc, synth, dev, steps):
     B.set_populations(pops)
     B.set_precision(rsc.PULSE_COMPENSATED)
     shape = B.autotune(sims(0, 1)[0])
+    adv_shape = B.advance_shape
     les = np.zeros((steps, count), np.int32)
     out = np.empty((steps, count, B.max_gates, 4), np.float32)
     bstream = torch.cuda.ExternalStream(B.stream)
@@ -451,6 +452,7 @@ def bench_batch(torch, rsc, synth, dev, steps):
                        "instance (speedup_vs_back_to_back).  Secondary: back to back with a blocking read of every "
                        "pulse as rs.c does, and with no pulse copied" % (total, GATES, steps))
     res["pulse_shape"] = {"warps": shape[0], "blocks_per_sm": shape[1]}
+    res["advance_shape"] = {"threads": adv_shape[0], "blocks_per_sm": adv_shape[1] or "all that fit"}
     res["scatterer_updates_per_s"] = bg / count * total
     return res
 

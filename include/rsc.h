@@ -261,9 +261,17 @@ int rsc_batch_set_precision(rsc_batch *b, int mode);
 
 /* Choose the batched pulse kernel's shape (warps per block 4 / 8 / 16 and
  * 1-4 resident blocks per SM) by timing it on the current state with the
- * given per-instance sim_descs (count x 16 floats, LES slot 0).  The state is
- * not changed. */
+ * given per-instance sim_descs (count x 16 floats, LES slot 0), then the
+ * background advance's shape (threads per block 64 / 128 / 256, with every
+ * block that fits resident or half of them) by timing it beside that pulse
+ * on scratch copies of the arrays it updates in place.  The state is not
+ * changed. */
 int rsc_batch_autotune(rsc_batch *b, const float *sim_descs);
+/* Set the batched background advance's shape directly: threads per block
+ * (64, 128 or 256) and resident blocks per SM (0: as many as fit). */
+int rsc_batch_set_advance_shape(rsc_batch *b, int threads, int blocks_per_sm);
+/* The batched background advance's shape (128, 0 until set or tuned). */
+int rsc_batch_get_advance_shape(rsc_batch *b, int *threads, int *blocks_per_sm);
 
 /* Run `steps` time steps of every instance: for step k and instance i the
  * pulse for sim_descs[(k * count + i) * 16 ...] is formed, then the instance

@@ -1741,6 +1741,11 @@ struct rsc_batch {
     int mode = RSC_PULSE_PLAIN;
     uint32_t Gmax = 0;
     int tune_warps = 0, tune_per_sm = 0;
+    /* background advance shape: threads per block and the shared-memory
+     * bytes each block asks for, which limits the resident blocks per SM
+     * (0: as many as fit) */
+    int adv_threads = rsc::kAdvanceThreads, adv_per_sm = 0;
+    size_t adv_smem = 0;
     bool tri = false;   /* the pulse kernel with the triangle range weight compiled in */
     /* per-instance launch descriptors and block prefixes */
     std::vector<rsc::BatchAdvance> h_adv;
@@ -1863,7 +1868,7 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
             A.dff[slot] = x->dff[slot];
         }
         b->h_rain_prefix[i] = acc_r;
-        acc_r += A.a.rain_blocks;
+        acc_r += (unsigned)((A.a.rain_count + (unsigned long long)b->adv_threads - 1) / (unsigned long long)b->adv_threads);
         b->h_deb_prefix[i] = acc_d;
         acc_d += blocks - A.a.rain_blocks;
         PulseArgs &P = b->h_pulse[i];
@@ -1939,6 +1944,43 @@ cudaError_t batch_launch_pulse(rsc_batch *b, int k) {
  * k for the pulse of step k - 1 (which read the pair it overwrites).  The
  * advance stream starts after the work queued on the batch's stream and the
  * batch's stream ends after it. */
+/* The background advance of one step of every instance at the batch's
+ * advance shape. */
+cudaError_t batch_launch_rain(rsc_batch *b, const rsc::BatchAdvance *adv, const rsc::BatchStep *st) {
+    const int n = (int)b->w.size();
+    const unsigned g = b->rain_blocks;
+    const size_t sm = b->adv_smem;
+    if (b->adv_threads == 64) {
+        rsc::k_advance_batch_rain<64><<<g, 64, sm, b->adv>>>(adv, st, b->d_rain_prefix, n);
+    } else if (b->adv_threads == 256) {
+        rsc::k_advance_batch_rain<256><<<g, 256, sm, b->adv>>>(adv, st, b->d_rain_prefix, n);
+    } else {
+        rsc::k_advance_batch_rain<128><<<g, 128, sm, b->adv>>>(adv, st, b->d_rain_prefix, n);
+    }
+    return cudaGetLastError();
+}
+
+/* Dynamic shared memory that leaves at most per_sm blocks of the batched
+ * background advance resident on an SM (0: no limit). */
+int batch_advance_smem(rsc_batch *b, int threads, int per_sm, size_t *smem) {
+    *smem = 0;
+    if (per_sm <= 0) return RSC_OK;
+    int dev = 0, sm_bytes = 0, optin = 0;
+    RSC_CUDA(cudaGetDevice(&dev));
+    RSC_CUDA(cudaDeviceGetAttribute(&sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    RSC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    size_t want = (size_t)sm_bytes / (size_t)per_sm + 1;
+    want = (want + 127) & ~(size_t)127;
+    if (want > (size_t)optin - 1024) want = (size_t)optin - 1024;
+    void *k = threads == 64 ? reinterpret_cast<void *>(rsc::k_advance_batch_rain<64>)
+                            : (threads == 256 ? reinterpret_cast<void *>(rsc::k_advance_batch_rain<256>)
+                                              : reinterpret_cast<void *>(rsc::k_advance_batch_rain<128>));
+    RSC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+    *smem = want;
+    (void)b;
+    return RSC_OK;
+}
+
 cudaError_t batch_enqueue(rsc_batch *b, int steps) {
     const int n = (int)b->w.size();
     const bool advance = b->rain_blocks || b->deb_blocks;
@@ -1973,9 +2015,7 @@ cudaError_t batch_enqueue(rsc_batch *b, int steps) {
             if (e != cudaSuccess) return e;
         }
         if (b->rain_blocks) {
-            rsc::k_advance_batch_rain<<<b->rain_blocks, rsc::kAdvanceThreads, 0, b->adv>>>(b->d_adv, st,
-                                                                                          b->d_rain_prefix, n);
-            e = cudaGetLastError();
+            e = batch_launch_rain(b, b->d_adv, st);
             if (e != cudaSuccess) return e;
         }
         if (b->deb_blocks) {
@@ -2293,6 +2333,130 @@ int rsc_batch_set_precision(rsc_batch *b, int mode) {
     return RSC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+/* The batched background advance's shape, timed as one step beside the
+ * batched pulse: threads per block 64 / 128 / 256, each with every block
+ * that fits resident and with half of them (shared memory asked for per
+ * block).  The advance writes the step's other pos / rcs pair, which the
+ * next run overwrites, and the arrays it updates in place (vel, rnd) are
+ * scratch copies here, so the state is not changed.  Without the memory for
+ * the copies the shape stays as it was. */
+int batch_tune_advance(rsc_batch *b) {
+    const size_t n = b->w.size();
+    if (b->rain_blocks == 0) return RSC_OK;
+    std::vector<size_t> off(n);
+    size_t total = 0;
+    for (size_t i = 0; i < n; i++) {
+        off[i] = total;
+        total += b->w[i]->numel;
+    }
+    float4 *svel = nullptr;
+    uint4 *srnd = nullptr;
+    rsc::BatchAdvance *sadv = nullptr;
+    cudaError_t e = cudaMalloc((void **)&svel, total * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&srnd, total * sizeof(uint4));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&sadv, n * sizeof(rsc::BatchAdvance));
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        free_ptr(svel);
+        free_ptr(srnd);
+        return RSC_OK;
+    }
+    std::vector<rsc::BatchAdvance> adv(b->h_adv);
+    int s = RSC_OK;
+    for (size_t i = 0; i < n && s == RSC_OK; i++) {
+        rsc_worker *x = b->w[i];
+        adv[i].a.vel = svel + off[i];
+        adv[i].a.rnd = srnd + off[i];
+        if (cudaMemcpyAsync(svel + off[i], x->vel, x->numel * sizeof(float4), cudaMemcpyDeviceToDevice, b->stream) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(srnd + off[i], x->rnd, x->numel * sizeof(uint4), cudaMemcpyDeviceToDevice, b->stream) !=
+                cudaSuccess) {
+            s = cuda_fail(RSC_ERR_CUDA, "advance tuning copies failed");
+        }
+    }
+    if (s == RSC_OK && cudaMemcpyAsync(sadv, adv.data(), n * sizeof(rsc::BatchAdvance), cudaMemcpyHostToDevice,
+                                       b->stream) != cudaSuccess) {
+        s = cuda_fail(RSC_ERR_CUDA, "advance tuning arguments");
+    }
+    EventPair ev;
+    if (s == RSC_OK && ev.init() != cudaSuccess) s = cuda_fail(RSC_ERR_CUDA, "advance tuning events");
+    float best = INFINITY;
+    int best_t = b->adv_threads, best_p = b->adv_per_sm;
+    const int shapes[6][2] = {{128, 0}, {64, 0}, {256, 0}, {128, 8}, {64, 16}, {256, 4}};
+    for (int c = 0; c < 6 && s == RSC_OK; c++) {
+        b->adv_threads = shapes[c][0];
+        b->adv_per_sm = shapes[c][1];
+        s = batch_advance_smem(b, b->adv_threads, b->adv_per_sm, &b->adv_smem);
+        if (s == RSC_OK) s = batch_prepare(b, b->h_steps);
+        if (s) break;
+        float ms = 0.0f;
+        for (int r = 0; r <= kTuneReps && s == RSC_OK; r++) {
+            cudaError_t q = cudaEventRecord(r == 1 ? ev.a : b->ev_afork, b->stream);
+            if (r == 1 && q == cudaSuccess) q = cudaEventRecord(b->ev_afork, b->stream);
+            if (q == cudaSuccess) q = cudaStreamWaitEvent(b->adv, b->ev_afork, 0);
+            if (q == cudaSuccess) q = batch_launch_pulse(b, 0);
+            if (q == cudaSuccess) q = batch_launch_rain(b, sadv, b->d_steps);
+            if (q == cudaSuccess) q = cudaEventRecord(b->ev_ba[0], b->adv);
+            if (q == cudaSuccess) q = cudaStreamWaitEvent(b->stream, b->ev_ba[0], 0);
+            if (q != cudaSuccess) s = cuda_fail(RSC_ERR_CUDA, "advance tuning step: %s", cudaGetErrorString(q));
+            b->launches += 2;
+        }
+        if (s) break;
+        if (cudaEventRecord(ev.b, b->stream) != cudaSuccess || cudaEventSynchronize(ev.b) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, ev.a, ev.b) != cudaSuccess) {
+            s = cuda_fail(RSC_ERR_CUDA, "advance tuning timing");
+            break;
+        }
+        if (ms < best) {
+            best = ms;
+            best_t = shapes[c][0];
+            best_p = shapes[c][1];
+        }
+    }
+    (void)cudaStreamSynchronize(b->stream);
+    free_ptr(svel);
+    free_ptr(srnd);
+    free_ptr(sadv);
+    if (s) return s;
+    b->adv_threads = best_t;
+    b->adv_per_sm = best_p;
+    s = batch_advance_smem(b, best_t, best_p, &b->adv_smem);
+    if (s == RSC_OK) s = batch_prepare(b, b->h_steps);
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsc_batch_set_advance_shape(rsc_batch *b, int threads, int blocks_per_sm) {
+    int s = check_batch(b);
+    if (s) return s;
+    if (threads != 64 && threads != 128 && threads != 256) return fail(RSC_ERR_ARG, "advance threads %d", threads);
+    if (blocks_per_sm < 0 || blocks_per_sm * threads > 2048) {
+        return fail(RSC_ERR_ARG, "advance blocks per SM %d at %d threads", blocks_per_sm, threads);
+    }
+    size_t smem = 0;
+    s = batch_advance_smem(b, threads, blocks_per_sm, &smem);
+    if (s) return s;
+    b->adv_threads = threads;
+    b->adv_per_sm = blocks_per_sm;
+    b->adv_smem = smem;
+    batch_drop_graph(b);
+    return RSC_OK;
+}
+
+int rsc_batch_get_advance_shape(rsc_batch *b, int *threads, int *blocks_per_sm) {
+    if (b == nullptr) return fail(RSC_ERR_ARG, "batch is NULL");
+    if (threads) *threads = b->adv_threads;
+    if (blocks_per_sm) *blocks_per_sm = b->adv_per_sm;
+    return RSC_OK;
+}
+
 int rsc_batch_autotune(rsc_batch *b, const float *sim_descs) {
     int s = check_batch(b);
     if (s) return s;
@@ -2335,6 +2499,9 @@ int rsc_batch_autotune(rsc_batch *b, const float *sim_descs) {
     }
     b->tune_warps = best_w;
     b->tune_per_sm = best_p;
+    s = batch_prepare(b, b->h_steps);
+    if (s == RSC_OK) s = batch_tune_advance(b);
+    if (s) return s;
     batch_drop_graph(b);
     RSC_CUDA(cudaEventRecord(b->ev_done, b->stream));
     for (rsc_worker *x : b->w) RSC_CUDA(cudaStreamWaitEvent(x->stream, b->ev_done, 0));

@@ -89,16 +89,19 @@ __device__ __forceinline__ int batch_advance_args(AdvanceArgs &sa, int &s_i, con
 }
 
 /* The background range of every instance (prefix over their background
- * blocks); the rain body chosen per instance by its concept.  A full SM of
- * resident threads (32 registers, 76 bytes spilled) measured 6% faster per
+ * blocks of T threads); the rain body chosen per instance by its concept.
+ * A full SM of resident threads (32 registers) measured 6% faster per
  * batched step than 6 blocks of 256 (40 registers), which had been faster
- * than 5: resident warps hide the texel loads' latency. */
-__global__ void __launch_bounds__(kAdvanceThreads, 2048 / kAdvanceThreads)
+ * than 5: resident warps hide the texel loads' latency.  T (64, 128, 256)
+ * and the resident blocks per SM (limited through dynamic shared memory)
+ * are the batch's advance shape, which rsc_batch_autotune times. */
+template <int T>
+__global__ void __launch_bounds__(T, 2048 / T)
 k_advance_batch_rain(const BatchAdvance *inst, const BatchStep *steps, const unsigned *prefix, int ninst) {
     __shared__ __align__(16) AdvanceArgs sa;
     __shared__ int s_i;
     const int i = batch_advance_args(sa, s_i, inst, steps, prefix, ninst);
-    const unsigned long long j = (unsigned long long)(blockIdx.x - __ldg(prefix + i)) * kAdvanceThreads + threadIdx.x;
+    const unsigned long long j = (unsigned long long)(blockIdx.x - __ldg(prefix + i)) * T + threadIdx.x;
     if (j >= sa.rain_count) return;
     const size_t x = (size_t)(sa.rain_origin + j);
     float4 pos, rcs;

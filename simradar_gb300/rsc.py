@@ -117,6 +117,8 @@ def load_library():
         "rsc_batch_set_populations": ([P, ctypes.POINTER(Population)], I),
         "rsc_batch_set_precision": ([P, I], I),
         "rsc_batch_set_persistent": ([P, I], I),
+        "rsc_batch_set_advance_shape": ([P, I, I], I),
+        "rsc_batch_get_advance_shape": ([P, ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "rsc_batch_autotune": ([P, _f32p], I),
         "rsc_batch_run": ([P, I, _f32p, ctypes.POINTER(ctypes.c_int32), _f32p, I], I),
         "rsc_batch_run_async": ([P, I, _f32p, ctypes.POINTER(ctypes.c_int32), _f32p, I], I),
@@ -422,6 +424,16 @@ class Batch:
 
     def set_precision(self, mode):
         _check(self._lib.rsc_batch_set_precision(self._h, int(mode)))
+
+    def set_advance_shape(self, threads, blocks_per_sm=0):
+        """The batched background advance's block size and resident blocks per SM."""
+        _check(self._lib.rsc_batch_set_advance_shape(self._h, int(threads), int(blocks_per_sm)))
+
+    @property
+    def advance_shape(self):
+        t, p = ctypes.c_int(0), ctypes.c_int(0)
+        _check(self._lib.rsc_batch_get_advance_shape(self._h, ctypes.byref(t), ctypes.byref(p)))
+        return t.value, p.value
 
     def set_persistent(self, enable):
         """Run every step of a run in one launch (rsc_batch_set_persistent)."""

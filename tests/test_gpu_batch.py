@@ -184,6 +184,33 @@ def test_batch_persistent_equals_graph(backend, oracle_lib, scenes, precision):
         o.close()
 
 
+def test_batch_advance_shapes(backend, scenes):
+    """The batched background advance at every block size and residency the
+    autotuner tries leaves the same state bit for bit, with the same pulses
+    (up to the order of the FP64 grid sums)."""
+    pops = [synth.population(S) for S in scenes]
+    ref = None
+    for shape in ((128, 0), (64, 0), (256, 4), (128, 8)):
+        ws = _workers(backend, scenes)
+        B = backend.Batch(ws)
+        B.set_populations(pops)
+        B.set_advance_shape(*shape)
+        assert B.advance_shape == shape
+        sims, les = _steps(scenes, 0, 3)
+        p = B.run(sims, les)
+        st = [W.download(STATE_FIELDS) for W in ws]
+        if ref is None:
+            ref = (p, st)
+        else:
+            scale = np.abs(ref[0]).max(axis=(2, 3), keepdims=True) + 1e-30
+            assert np.all(np.abs(p - ref[0]) <= 1e-6 * scale), shape
+            for a, r in zip(st, ref[1]):
+                for f in STATE_FIELDS:
+                    assert np.array_equal(bits(a[f]), bits(r[f])), (shape, f)
+        for o in [B] + ws:
+            o.close()
+
+
 def test_batch_autotune_and_compensated(backend, oracle_lib, scenes):
     """The autotuner picks a reachable shape and leaves the state alone; the
     compensated form in a batch keeps its bound against FP64."""
@@ -195,6 +222,8 @@ def test_batch_autotune_and_compensated(backend, oracle_lib, scenes):
     sims, les = _steps(scenes, 0, 2)
     warps, per_sm = B.autotune(sims[0])
     assert warps in (4, 8, 16) and 1 <= per_sm <= 4
+    threads, adv_per_sm = B.advance_shape
+    assert threads in (64, 128, 256) and adv_per_sm in (0, 1024 // threads)
     for i, W in enumerate(ws):
         assert_state_equal(W.download(STATE_FIELDS), scenes[i].state, where="instance %d after autotune " % i)
     sts = [O.OracleState(S.state) for S in scenes]
