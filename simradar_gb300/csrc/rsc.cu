@@ -88,6 +88,7 @@ struct rsc_worker {
     double *rk64 = nullptr;
     double *acc64 = nullptr;      /* the pulse kernel's FP64 grid accumulator */
     unsigned *counter = nullptr;
+    unsigned long long *runs = nullptr;   /* the compensated pulse's run counter */
     /* tables */
     float *range_weight = nullptr;
     uint32_t range_n = 0;
@@ -280,6 +281,7 @@ void free_arrays(rsc_worker *w) {
     free_ptr(w->rk64);
     free_ptr(w->acc64);
     free_ptr(w->counter);
+    free_ptr(w->runs);
     free_sort(w);
     w->pos = w->vel = w->ori = w->tum = w->aux = w->rcs = w->sig = w->pulse = nullptr;
     w->rnd = nullptr;
@@ -288,6 +290,7 @@ void free_arrays(rsc_worker *w) {
     w->rk64 = nullptr;
     w->acc64 = nullptr;
     w->counter = nullptr;
+    w->runs = nullptr;
     w->num_scats = w->numel = 0;
 }
 
@@ -798,6 +801,8 @@ int rsc_worker_malloc(rsc_worker *w, size_t num_scats, float range_start, float 
     RSC_CUDA(cudaMemsetAsync(w->acc64, 0, range_count * 4 * sizeof(double), w->stream));
     RSC_CUDA(cudaMalloc((void **)&w->counter, sizeof(unsigned)));
     RSC_CUDA(cudaMemsetAsync(w->counter, 0, sizeof(unsigned), w->stream));
+    RSC_CUDA(cudaMalloc((void **)&w->runs, sizeof(unsigned long long)));
+    RSC_CUDA(cudaMemsetAsync(w->runs, 0, sizeof(unsigned long long), w->stream));
     s = set_gates(w);
     if (s) return s;
     RSC_CUDA(cudaStreamSynchronize(w->stream));
@@ -1565,6 +1570,7 @@ int rsc_make_pulse(rsc_worker *w, const float sim_desc[16]) {
         /* the error-free warp sums need the grouped path, whatever the order */
         P.coherent_span = (int)w->G + 1;
         P.mom_n = w->moments ? moment_span(P) : 0;
+        P.runs = w->runs;
     }
     const bool mat = (mode == RSC_PULSE_PLAIN) && (w->materialize || sim_desc[15] != 0.0f);
     P.materialize = mat ? 1 : 0;
@@ -1877,6 +1883,7 @@ int batch_prepare(rsc_batch *b, const rsc::BatchStep *row) {
             P.rk = x->rk_hi;
             P.coherent_span = (int)x->G + 1;
             P.mom_n = x->moments ? moment_span(P) : 0;
+            P.runs = x->runs;
         }
         P.materialize = 0;
         tri = tri && P.rw_tri;
@@ -2158,6 +2165,7 @@ int rsc_autotune(rsc_worker *w, const float sim_desc[16], int *warps_out, int *b
         P.rk = w->rk_hi;
         P.coherent_span = (int)w->G + 1;
         P.mom_n = w->moments ? moment_span(P) : 0;
+        P.runs = w->runs;
     }
     P.materialize = 0;
     s = pulse_d2h_wait(w);

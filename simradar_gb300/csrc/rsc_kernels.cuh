@@ -479,6 +479,7 @@ struct PulseArgs {
                           * summed per range interval as moments (PulseBins::add_k), 0 otherwise */
     double *acc64;       /* G * 4 FP64 accumulators, zero between launches */
     unsigned *counter;
+    unsigned long long *runs;   /* the grouped compensated pulse's run counter, zero between launches (or null) */
     float4 *pulse;
     double *pulse64;
 };

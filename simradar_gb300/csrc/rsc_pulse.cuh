@@ -1133,7 +1133,10 @@ struct PulseBins {
             if (MODE == 2) P.pulse64[o] = v;
             P.acc64[o] = 0.0;
         }
-        if (threadIdx.x == 0) *P.counter = 0u;
+        if (threadIdx.x == 0) {
+            *P.counter = 0u;
+            if (P.runs != nullptr) *P.runs = 0ull;
+        }
     }
 };
 
@@ -1168,35 +1171,52 @@ __global__ void __launch_bounds__(512) k_pulse(const PulseArgs P) {
  * order, K scatterers per lane (PulseBins::add_k): warp w of a block takes
  * runs of 32 K neighbours. */
 template <int MODE, int K, int TRI = -1>
+__device__ __forceinline__ void pulse_group_run(const PulseArgs &P, PulseBins<MODE, 1> &B, unsigned long long base) {
+    const unsigned long long n = P.n;
+    bool in[K];
+    unsigned long long idx[K];
+    float4 pp[K], xx[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        idx[q] = base + 32u * q + B.lane;
+        in[q] = idx[q] < n;
+        pp[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        xx[q] = pp[q];
+        if (in[q]) {
+            pp[q] = __ldg(P.pos + idx[q]);
+            xx[q] = __ldg(P.rcs + idx[q]);
+        }
+    }
+    B.template add_k<K, TRI>(P, in, idx, pp, xx);
+}
+
+/* Warps take runs of 32 K neighbours: in fixed strides, or -- the
+ * compensated form, whose sums are exact in any order -- the next run from
+ * a counter as each finishes its last, so that the block's warps reach its
+ * final sums together instead of some idling at the barrier while others do
+ * one more run (the counter is left at zero by the last block). */
+template <int MODE, int K, int TRI = -1>
 __device__ __forceinline__ void pulse_body_group(const PulseArgs &P, unsigned blk, unsigned nblk) {
     PulseBins<MODE, 1> B;
     B.init(P);
-    const unsigned long long stride = (unsigned long long)K * nblk * blockDim.x;
     const unsigned long long n = P.n;
-    const unsigned long long base0 = (unsigned long long)K * ((unsigned long long)blk * blockDim.x + (threadIdx.x & ~31u));
-    for (unsigned long long base = base0; base < n; base += stride) {
-        bool in[K];
-        unsigned long long idx[K];
-        float4 pp[K], xx[K];
-#pragma unroll
-        for (int q = 0; q < K; q++) {
-            idx[q] = base + 32u * q + B.lane;
-            in[q] = idx[q] < n;
-            pp[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            xx[q] = pp[q];
-            if (in[q]) {
-                pp[q] = __ldg(P.pos + idx[q]);
-                xx[q] = __ldg(P.rcs + idx[q]);
-            }
+    if (MODE == 1 && P.runs != nullptr) {
+        const unsigned long long runs_n = (n + 32ull * K - 1) / (32ull * K);
+        for (;;) {
+            unsigned long long r = 0;
+            if (B.lane == 0) r = atomicAdd(P.runs, 1ull);
+            r = __shfl_sync(0xffffffffu, r, 0);
+            if (r >= runs_n) break;
+            pulse_group_run<MODE, K, TRI>(P, B, r * 32ull * K);
         }
-        B.template add_k<K, TRI>(P, in, idx, pp, xx);
+    } else {
+        const unsigned long long stride = (unsigned long long)K * nblk * blockDim.x;
+        const unsigned long long base0 =
+            (unsigned long long)K * ((unsigned long long)blk * blockDim.x + (threadIdx.x & ~31u));
+        for (unsigned long long base = base0; base < n; base += stride) pulse_group_run<MODE, K, TRI>(P, B, base);
     }
     B.finish(P, nblk);
 }
-
-/* The plain or compensated pulse over a state in spatial order, K
- * scatterers per lane; TRI 1 when the range table is the triangle (its
- * closed form compiled in, no table test per gate). */
 template <int MODE, int K, int TRI = -1>
 __global__ void __launch_bounds__(512) k_pulse_group(const PulseArgs P) {
     pulse_body_group<MODE, K, TRI>(P, blockIdx.x, gridDim.x);
