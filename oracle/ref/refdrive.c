@@ -19,7 +19,9 @@
  *     ellipsoid RCS, ADM and RCS images, LES descriptor, population layout,
  *     radar parameters, DSD), read back from the device objects;
  *   - the event list: state uploads, LES frame writes (slot, frame), time
- *     advances (with the simulation descriptor and LES slot the kernels got),
+ *     advances (with the simulation descriptor and LES slot the kernels got,
+ *     and with concept bit 7 the debris flux field table and descriptor
+ *     db_atts read, as an index into dff_tables / dff_descs),
  *     debris RCS refreshes and pulses (descriptor, the pulse rs.c read back,
  *     the merged pulse with its gain, and the oracle's per-gate sums of |term|
  *     for the tolerance);
@@ -62,6 +64,13 @@ static uint64_t g_init_hash[8];
 static int g_uploads;
 static uint64_t g_deb_launch[8][4];
 static int g_ndeb = -1;
+/* debris flux field tables db_atts was given (concept bit 7), each kept once
+ * in the order first seen, with the descriptor it came with */
+#define MAX_DFF 64
+static float *g_dff_tab[MAX_DFF];
+static float g_dff_desc[MAX_DFF][16];
+static size_t g_dff_n;
+static int g_ndff;
 static int g_adv_deb;         /* debris launches in the current advance */
 static int g_fail;
 
@@ -165,6 +174,36 @@ static void hook(const clshim_event *ev, void *user) {
                 fprintf(stderr, "refdrive: debris launch %d changed between advances\n", g_adv_deb);
                 g_fail = 1;
             }
+        }
+        if (H->sim_concept & RSSimulationConceptDebrisFluxFromVelocity) {
+            /* the table (argument 15, dff_icdf[les_id]) and its descriptor
+             * (16) this launch reads, recorded against the advance */
+            cl_mem dm;
+            float dd[16];
+            size_t bytes = 0;
+            clshim_kernel_arg(ev->kernel, 15, &dm, sizeof(dm));
+            clshim_kernel_arg(ev->kernel, 16, dd, sizeof(dd));
+            const float *tab = (const float *)clshim_mem_data(dm, &bytes, NULL);
+            const size_t n = bytes / sizeof(float);
+            int idx = -1;
+            if (g_ndff > 0 && n == g_dff_n && !memcmp(g_dff_tab[g_ndff - 1], tab, bytes) &&
+                !memcmp(g_dff_desc[g_ndff - 1], dd, sizeof(dd))) {
+                idx = g_ndff - 1;
+            } else if (g_ndff < MAX_DFF && (g_ndff == 0 || n == g_dff_n)) {
+                g_dff_tab[g_ndff] = (float *)malloc(bytes);
+                memcpy(g_dff_tab[g_ndff], tab, bytes);
+                memcpy(g_dff_desc[g_ndff], dd, sizeof(dd));
+                g_dff_n = n;
+                idx = g_ndff++;
+            } else {
+                fprintf(stderr, "refdrive: debris flux field tables beyond %d or of changing size\n", MAX_DFF);
+                g_fail = 1;
+            }
+            if (e->i[3] >= 0 && e->i[3] != idx) {
+                fprintf(stderr, "refdrive: debris launches of one advance read different flux tables\n");
+                g_fail = 1;
+            }
+            e->i[3] = idx;
         }
         float sd[16];
         clshim_kernel_arg(ev->kernel, 17, sd, sizeof(sd));
@@ -407,6 +446,13 @@ int main(int argc, char **argv) {
         put_f1(nm, C->rcs_desc[r].s, 16);
     }
     put_f1("dff_desc", C->dff_desc.s, 16);
+    if (g_ndff > 0) {
+        float *all = (float *)malloc((size_t)g_ndff * g_dff_n * sizeof(float));
+        for (int k = 0; k < g_ndff; k++) memcpy(all + (size_t)k * g_dff_n, g_dff_tab[k], g_dff_n * sizeof(float));
+        put("dff_tables", "f4", all, (size_t)g_ndff * g_dff_n * 4, 2, g_ndff, g_dff_n, 0, 0);
+        put("dff_descs", "f4", g_dff_desc, (size_t)g_ndff * 64, 2, g_ndff, 16, 0, 0);
+        free(all);
+    }
     /* events */
     uint32_t *kinds = (uint32_t *)malloc((size_t)g_nev * 4);
     int32_t *ints = (int32_t *)malloc((size_t)g_nev * 16);

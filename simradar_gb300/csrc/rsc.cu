@@ -1032,7 +1032,7 @@ int rsc_set_dff(rsc_worker *w, int slot, const float *icdf, uint32_t n, const fl
     if (s) return s;
     if (slot < 0 || slot > 1 || icdf == nullptr || desc == nullptr || n == 0) return fail(RSC_ERR_ARG, "DFF table");
     /* db_atts reads icdf[floor(clamp(r * sf + {0, 1}, 0, sf))] (rs.cl:799-805) */
-    if (!(desc[15] >= 0.0f) || (uint32_t)desc[15] >= n) return fail(RSC_ERR_ARG, "DFF max index %g >= %u", desc[15], n);
+    if (!(desc[15] >= 0.0f && desc[15] < (float)n)) return fail(RSC_ERR_ARG, "DFF max index %g >= %u", desc[15], n);
     cudaStreamSynchronize(w->stream);
     s = upload_floats(&w->dff[slot], icdf, n);
     if (s) return s;

@@ -271,6 +271,14 @@ int main(int argc, char **argv) {
     float *merged = (float *)calloc(P * G * 4, sizeof(float));
     uint64_t upload_hash[8] = {0}, les_hash[64][2];
     int nles = 0;
+    /* the debris flux field tables rs.c derived from each LES frame (concept
+     * bit 7): each advance names the one its debris launches read, which
+     * goes into the advance's LES slot as rs.c's dff_icdf[les_id] */
+    const Rec *dt = find("dff_tables");
+    const float *dff_tab = dt ? (const float *)dt->data : NULL;
+    const float *dff_desc = dt ? (const float *)need("dff_descs") : NULL;
+    const uint32_t dff_n = dt ? (uint32_t)dt->shape[1] : 0u;
+    int dff_set[2] = {-1, -1};
     for (size_t e = 0; e < nev; e++) {
         const int32_t *iv = ints + 4 * e;
         const float *sd = descs + 16 * e;
@@ -297,6 +305,10 @@ int main(int argc, char **argv) {
                 break;
             }
             case EV_ADVANCE:
+                if (iv[3] >= 0 && dff_tab != NULL && dff_set[iv[0] & 1] != iv[3]) {
+                    CHECK(rsc_set_dff(w, iv[0], dff_tab + (size_t)iv[3] * dff_n, dff_n, dff_desc + 16 * (size_t)iv[3]));
+                    dff_set[iv[0] & 1] = iv[3];
+                }
                 CHECK(rsc_advance_time(w, &pop, iv[0], sd));
                 break;
             case EV_DEBRIS_RCS:

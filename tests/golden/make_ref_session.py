@@ -13,7 +13,7 @@ descriptors, population layout, the event list with every descriptor), the
 pulses it read back, and hashes of the uploaded state, of every LES frame
 and of the final state (tests/test_ref_session.py, tests/test_gpu_ref_session.py).
 
-    python tests/golden/make_ref_session.py
+    python tests/golden/make_ref_session.py [session ...]
 """
 import os
 import sys
@@ -30,13 +30,18 @@ from simradar_gb300 import synth  # noqa: E402
 
 # name: refdrive arguments.  Concepts (rs_enum.h:127-137): 26 = dragged +
 # bounded + uniform-DSD (simradar's default DBU); 9 = bounded + cross-pol
-# (bg_atts for the background).
+# (bg_atts for the background); 154 = DBU + debris flux from velocity (rs.c
+# derives the flux field from every LES frame it sets, rs.c:3106-3111, and
+# respawned debris take their cell from it).
 SESSIONS = {
     "ref_session_dbu": dict(density=0.3, pulses=40, warmup=130, seed=19760520, gate=30.0,
                             scan="P:3.0,-12:12:0.24", concept=26,
                             debris=[(synth.OBJ_LEAF, 256), (synth.OBJ_WOODBOARD_2X4, 256), (synth.OBJ_BRICK, 256)]),
     "ref_session_bg": dict(density=0.2, pulses=24, warmup=0, seed=4321, gate=15.0,
                            scan="R:2.0,1:15:0.5", concept=9, debris=[(synth.OBJ_BRICK, 300)]),
+    "ref_session_dff": dict(density=0.1, pulses=16, warmup=400, seed=2468, gate=30.0,
+                            scan="P:3.0,-12:12:0.24", concept=154,
+                            debris=[(synth.OBJ_LEAF, 512), (synth.OBJ_BRICK, 512)]),
 }
 TABLES = dict(seed=7, volumes_per_file=10, adm_dims=(37, 19), rcs_dims=(37, 19))
 
@@ -61,10 +66,11 @@ def record(name, home, work):
 
 
 def main():
+    names = sys.argv[1:] or list(SESSIONS)   # record all, or the sessions named
     refbind.build()
     with tempfile.TemporaryDirectory() as home, tempfile.TemporaryDirectory() as work:
         write_tables(home)
-        for name in SESSIONS:
+        for name in names:
             out = record(name, home, work)
             path = os.path.join(HERE, name + ".npz")
             np.savez_compressed(path, **out)

@@ -11,7 +11,8 @@ These CPU tests check against those recordings:
     state (rsc_populate_host, the backend's own);
   * that the oracle's Python orchestration (oracle/oracle.py, the checker of
     every GPU parity test) replays rs.c's event list to the same pulses and
-    the same final state, bit for bit;
+    the same final state, bit for bit (with the debris flux field tables rs.c
+    derived from each LES frame in the session with that concept);
   * where the reference tree is present, that the recording is reproduced.
 """
 import math
@@ -26,7 +27,7 @@ from simradar_gb300 import rsc, synth
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-SESSIONS = ["ref_session_dbu", "ref_session_bg"]
+SESSIONS = ["ref_session_dbu", "ref_session_bg", "ref_session_dff"]
 FIELDS = ["pos", "vel", "ori", "tum", "aux", "rcs", "sig", "rnd"]
 EV_LES, EV_ADVANCE, EV_DEBRIS_RCS, EV_PULSE, EV_UPLOAD = 1, 2, 3, 4, 5
 
@@ -55,6 +56,12 @@ class SessionScene:
         self.rcs_tables = [(R["rcs_real_%d" % r], R["rcs_imag_%d" % r], R["rcs_desc_%d" % r])
                            for r in range(int(R["rcs_count"]))]
         self.counts = [int(c) for c in R["counts"][:int(R["num_types"])]]
+        self.dff, self.dff_desc = None, np.zeros(16, np.float32)
+
+    def use_dff(self, R, index):
+        """The debris flux field table (and descriptor) an advance read."""
+        if index >= 0:
+            self.dff, self.dff_desc = R["dff_tables"][index], R["dff_descs"][index]
 
 
 def populate_args(R):
@@ -179,6 +186,7 @@ def replay_oracle(R, les_dir):
                 uvwt, cpxx, _ = src.read(int(ints[1]))
                 vols[int(ints[0])] = synth.LESVolume(uvwt, cpxx)
             elif kind == EV_ADVANCE:
+                S.use_dff(R, int(ints[3]))
                 O.advance_time(st, S, S.counts, vols[int(ints[0])], desc)
             elif kind == EV_DEBRIS_RCS:
                 O.db_rcs(st, S, S.counts, desc)
