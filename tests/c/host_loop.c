@@ -1,7 +1,8 @@
 /*
  * host_loop.c -- a C99 host that drives the backend through include/rsc.h
- * exactly as rs.c would after the integration (the call-site map of
- * INTEGRATION.md), replaying a session recorded from the reference host.
+ * exactly as rs.c would after the integration (each rs.c step below mapped
+ * to the calls that replace its OpenCL block), replaying a session recorded
+ * from the reference host.
  *
  * Input (argv[1]): a record file (RSREF001 format, written by
  * tests/test_gpu_ref_session.py from tests/golden/ref_session_*.npz): the
@@ -20,8 +21,8 @@
  *   rsc_download_pulse (gain 1, and the gain of RS_merge_pulse_tmp)
  *   rsc_download                                       RS_download
  *
- * The population block is INTEGRATION.md's (the round-robin ADM / RCS table
- * indices of rs.c:5351-5373).  Output: the pulses read back, the merged and
+ * The population block follows rs.c's type ranges and the round-robin
+ * ADM / RCS table indices of rs.c:5351-5373.  Output: the pulses read back, the merged and
  * scaled pulses, FNV-1a hashes of the uploaded state, of every LES frame
  * read and of the final state, and the final state every 8th scatterer.
  */
@@ -219,7 +220,7 @@ int main(int argc, char **argv) {
     const size_t nn = (size_t)info.nx * info.ny * info.nz;
     float *uvwt = (float *)malloc(nn * 16), *cpxx = (float *)malloc(nn * 16);
 
-    /* the population block of INTEGRATION.md (rs.c:5351-5373) */
+    /* the population: rs.c's type ranges and table indices (rs.c:5351-5373) */
     rsc_population pop;
     memset(&pop, 0, sizeof(pop));
     int a = 0, r = 0;

@@ -273,6 +273,29 @@ def test_compensated_moments_and_per_gate(backend, oracle_lib, scene_db):
     W.close()
 
 
+@pytest.mark.parametrize("concept", [synth.CONCEPT_DBU, 0])
+def test_advance_two_per_thread(backend, oracle_lib, scene_db, concept):
+    """Two background scatterers per advance thread (rsc_set_advance_shape)
+    advance the state bit for bit as the oracle does, el_atts and bg_atts,
+    respawns included."""
+    O = oracle_lib
+    S = scene_db
+    pop = synth.population(S)
+    W = backend.Worker(0)
+    synth.load_worker(W, S)
+    W.set_advance_shape(2)
+    st = O.OracleState(S.state)
+    for k in range(4):
+        sd = synth.pulse_sim_desc(S, k, tic=k * 1e-3)
+        sd[5] = synth.fbits(concept)
+        W.make_pulse(sd)
+        W.advance_time(pop, 0, sd)
+        O.advance_time(st, S, S.counts, S.les[0], sd)
+        assert_state_equal(W.download(STATE_FIELDS), st.s, where="step %d " % k)
+    assert (bits(st.s["rnd"]) != bits(S.state["rnd"])).any(axis=1).sum() >= 64
+    W.close()
+
+
 def test_dense_gate_path(backend, oracle_lib):
     """A range weight with non-zero edges reaches every gate (dense path)."""
     S = synth.make_scene(num_rain=5000, les_count=1)

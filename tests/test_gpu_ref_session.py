@@ -2,7 +2,7 @@
 host through the C ABI (tests/c/host_loop.c, compiled here with gcc against
 include/rsc.h and libsimradar_gb300.so).
 
-The host makes the calls rs.c makes after the integration (INTEGRATION.md):
+The host makes the calls rs.c makes after the integration:
 the worker, the tables and descriptors rs.c derived, the LES frames read by
 the backend's reader from the same tables folder (rewritten here, the same
 bytes) with the first one set synchronously and the swap uploaded on the copy
