@@ -32,7 +32,9 @@ from simradar_gb300 import synth  # noqa: E402
 # bounded + uniform-DSD (simradar's default DBU); 9 = bounded + cross-pol
 # (bg_atts for the background); 154 = DBU + debris flux from velocity (rs.c
 # derives the flux field from every LES frame it sets, rs.c:3106-3111, and
-# respawned debris take their cell from it).
+# respawned debris take their cell from it); 90 = DBU + vertically pointing
+# radar (rs.c's scan box and gates for a radar looking up, rs.c:1602-1640,
+# rs.c:2143-2160, rs.c:5830-5860).
 SESSIONS = {
     "ref_session_dbu": dict(density=0.3, pulses=40, warmup=130, seed=19760520, gate=30.0,
                             scan="P:3.0,-12:12:0.24", concept=26,
@@ -42,6 +44,8 @@ SESSIONS = {
     "ref_session_dff": dict(density=0.1, pulses=16, warmup=400, seed=2468, gate=30.0,
                             scan="P:3.0,-12:12:0.24", concept=154,
                             debris=[(synth.OBJ_LEAF, 512), (synth.OBJ_BRICK, 512)]),
+    "ref_session_vpr": dict(density=0.3, pulses=24, warmup=60, seed=97531, gate=30.0,
+                            scan="P:90.0,0:360:1.0", concept=90, debris=[(synth.OBJ_LEAF, 128)]),
 }
 TABLES = dict(seed=7, volumes_per_file=10, adm_dims=(37, 19), rcs_dims=(37, 19))
 

@@ -27,7 +27,7 @@ from simradar_gb300 import rsc, synth
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-SESSIONS = ["ref_session_dbu", "ref_session_bg", "ref_session_dff"]
+SESSIONS = ["ref_session_dbu", "ref_session_bg", "ref_session_dff", "ref_session_vpr"]
 FIELDS = ["pos", "vel", "ori", "tum", "aux", "rcs", "sig", "rnd"]
 EV_LES, EV_ADVANCE, EV_DEBRIS_RCS, EV_PULSE, EV_UPLOAD = 1, 2, 3, 4, 5
 
@@ -156,7 +156,11 @@ def test_beam_positions_match(name):
     RS_populate advances the beam to position 0 before its warm pulse, and
     the loop advances it after each pulse.  (With no warm-up advance between
     them, rs.c forms no new pulse for loop pulse 0 -- the signal needs no
-    update -- and reads back RS_populate's.)"""
+    update -- and reads back RS_populate's.)  Bit for bit, except with the
+    beam at 90 degrees elevation: there cos(el) is 4e-8, and the C
+    library's cosf / sinf and numpy's float32 ones give the horizontal
+    components within 2 ulps of each other (the GPU replays take rs.c's own
+    descriptors)."""
     R = load(name)
     scan = str(R["meta_scan"])
     mode, rest = scan.split(":", 1)
@@ -167,7 +171,12 @@ def test_beam_positions_match(name):
         k = int(R["ev_int"][i, 0])
         az, el = pos[max(k, 0) % len(pos)]
         want = np.array(synth.beam_unit(az, el), np.float32)
-        assert np.array_equal(bits(R["ev_desc"][i, :3]), bits(want)), (k, R["ev_desc"][i, :3], want)
+        got = R["ev_desc"][i, :3]
+        if el == 90.0:
+            ulps = np.abs(bits(got).astype(np.int64) - bits(want).astype(np.int64))
+            assert np.all(ulps <= 2) and bits(got)[2] == bits(want)[2], (k, got, want)
+        else:
+            assert np.array_equal(bits(got), bits(want)), (k, got, want)
 
 
 def replay_oracle(R, les_dir):
