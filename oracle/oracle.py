@@ -103,11 +103,12 @@ class OracleState:
         return self.s[k]
 
 
-def advance_time(st, S, pop_counts, les_vol, sim_desc):
+def advance_time(st, S, pop_counts, les_vol, sim_desc, L=None):
     """RS_advance_time's launches (rs.c:5325-5374) on the oracle.  Type 0 uses
     el_atts / fp_atts / bg_atts by concept; debris type k uses ADM / RCS table
-    k - 1; the DFF slot is unused unless concept C is set."""
-    L = lib()
+    k - 1; the DFF slot is unused unless concept C is set.  L: another library
+    with the oracle's entry points (refbind.rscl(), the reference's rs.cl)."""
+    L = L or lib()
     s = st.s
     sd = np.ascontiguousarray(sim_desc, dtype=np.float32)
     concept = int(np.frombuffer(sd[5:6].tobytes(), dtype=np.uint32)[0])
@@ -140,8 +141,8 @@ def advance_time(st, S, pop_counts, les_vol, sim_desc):
         origin += n
 
 
-def db_rcs(st, S, pop_counts, sim_desc):
-    L = lib()
+def db_rcs(st, S, pop_counts, sim_desc, L=None):
+    L = L or lib()
     s = st.s
     sd = np.ascontiguousarray(sim_desc, dtype=np.float32)
     origin = pop_counts[0]
@@ -153,10 +154,11 @@ def db_rcs(st, S, pop_counts, sim_desc):
         origin += n
 
 
-def make_pulse(st, S, sim_desc, group_size_multiple=64, max_work_group_size=1024, local_mem=49152, name_swap=1):
+def make_pulse(st, S, sim_desc, group_size_multiple=64, max_work_group_size=1024, local_mem=49152, name_swap=1,
+               L=None):
     """scat_sig_aux + pass 1 + pass 2 as RS_make_pulse enqueues them; returns the
     unscaled pulse (range_count, 4).  Updates sig / aux in the state."""
-    L = lib()
+    L = L or lib()
     s = st.s
     N = s["pos"].shape[0]
     pulse = np.zeros((S.range_count, 4), dtype=np.float32)

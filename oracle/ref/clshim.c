@@ -11,8 +11,11 @@
  * sequence produces.  Nothing in the simradar_gb300 package loads it.
  *
  * The one "device" it offers runs each rs.cl kernel rs.c enqueues with the
- * oracle's restatement of that kernel (oracle/rsoracle.c), chosen by the
- * kernel's source name (so the pass-2 name swap of rs.c:506-507 is kept),
+ * oracle's restatement of that kernel (oracle/rsoracle.c) or, after
+ * clshim_set_kernels(CLSHIM_KERNELS_RSCL) (or with CLSHIM_KERNELS=rscl in the
+ * environment), with the reference's own rs.cl kernel compiled for the CPU
+ * (oracle/ref/rscl.h), chosen by the kernel's source name (so the pass-2 name
+ * swap of rs.c:506-507 is kept),
  * with the arguments rs.c set by index (the argument lists of rs.cl:374-1453
  * and the index enums of rs_priv.h:13-80) and the global offset and size of
  * the launch (rs.c:5342-5369).  Buffers and images live in host memory;
@@ -32,6 +35,7 @@
 #include "CL/cl.h"
 #include "CL/cl_gl.h"
 #include "rsoracle.h"
+#include "rscl.h"
 #include "clshim.h"
 
 struct _cl_platform_id { int unused; };
@@ -552,6 +556,20 @@ static int check_args(cl_kernel k) {
     return 0;
 }
 
+/* which kernels the device runs: the oracle's restatement or the
+ * reference's rs.cl (CLSHIM_KERNELS=rscl selects the latter at start) */
+static int g_kernels = -1;
+
+void clshim_set_kernels(int which) { g_kernels = which; }
+
+static int kernels_rscl(void) {
+    if (g_kernels < 0) {
+        const char *e = getenv("CLSHIM_KERNELS");
+        g_kernels = (e != NULL && !strcmp(e, "rscl")) ? CLSHIM_KERNELS_RSCL : CLSHIM_KERNELS_ORACLE;
+    }
+    return g_kernels == CLSHIM_KERNELS_RSCL;
+}
+
 cl_int clEnqueueNDRangeKernel(cl_command_queue q, cl_kernel k, cl_uint dim, const size_t *goff, const size_t *gsize,
                               const size_t *lsize, cl_uint nw, const cl_event *wl, cl_event *ev) {
     (void)q; (void)nw; (void)wl;
@@ -563,35 +581,38 @@ cl_int clEnqueueNDRangeKernel(cl_command_queue q, cl_kernel k, cl_uint dim, cons
     const size_t local = lsize ? lsize[0] : 0;
     const char *n = k->name;
     notify(CLSHIM_LAUNCH, NULL, 0, 0, NULL, k, origin, count, local);
+    const int ref = kernels_rscl();
     if (!strcmp(n, "bg_atts") || !strcmp(n, "el_atts")) {
         if (origin + count > buf_n16(k, 0)) return CL_INVALID_GLOBAL_OFFSET;
         void (*f)(of4 *, of4 *, of4 *, ou4 *, or_image, const float *, const of4 *, const float *, const float *,
-                  size_t, size_t) = n[0] == 'b' ? or_bg_atts : or_el_atts;
+                  size_t, size_t) = n[0] == 'b' ? (ref ? rscl_bg_atts : or_bg_atts) : (ref ? rscl_el_atts : or_el_atts);
         f((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), (ou4 *)buf(k, 3), img(k, 4), val_f(k, 6),
           (const of4 *)buf(k, 7), val_f(k, 8), val_f(k, 9), origin, count);
     } else if (!strcmp(n, "fp_atts")) {
         if (origin + count > buf_n16(k, 0)) return CL_INVALID_GLOBAL_OFFSET;
-        or_fp_atts((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), img(k, 4), img(k, 5), val_f(k, 6),
-                   val_f(k, 9), origin, count);
+        (ref ? rscl_fp_atts : or_fp_atts)((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), img(k, 4), img(k, 5),
+                                          val_f(k, 6), val_f(k, 9), origin, count);
     } else if (!strcmp(n, "db_atts")) {
         if (origin + count > buf_n16(k, 0)) return CL_INVALID_GLOBAL_OFFSET;
-        or_db_atts((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), (of4 *)buf(k, 3), (of4 *)buf(k, 4),
-                   (ou4 *)buf(k, 5), img(k, 6), val_f(k, 8), img(k, 9), img(k, 10), val_f(k, 11), img(k, 12),
-                   img(k, 13), val_f(k, 14), (const float *)buf(k, 15), val_f(k, 16), val_f(k, 17), origin, count);
+        (ref ? rscl_db_atts : or_db_atts)((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), (of4 *)buf(k, 3),
+                                          (of4 *)buf(k, 4), (ou4 *)buf(k, 5), img(k, 6), val_f(k, 8), img(k, 9),
+                                          img(k, 10), val_f(k, 11), img(k, 12), img(k, 13), val_f(k, 14),
+                                          (const float *)buf(k, 15), val_f(k, 16), val_f(k, 17), origin, count);
     } else if (!strcmp(n, "db_rcs")) {
         if (origin + count > buf_n16(k, 0)) return CL_INVALID_GLOBAL_OFFSET;
-        or_db_rcs((const of4 *)buf(k, 0), (const of4 *)buf(k, 1), (of4 *)buf(k, 2), img(k, 3), img(k, 4),
-                  val_f(k, 5), val_f(k, 6), origin, count);
+        (ref ? rscl_db_rcs : or_db_rcs)((const of4 *)buf(k, 0), (const of4 *)buf(k, 1), (of4 *)buf(k, 2), img(k, 3),
+                                        img(k, 4), val_f(k, 5), val_f(k, 6), origin, count);
     } else if (!strcmp(n, "scat_sig_aux")) {
         if (origin != 0 || count > buf_n16(k, 0)) return CL_INVALID_GLOBAL_OFFSET;
-        or_scat_sig_aux((of4 *)buf(k, 0), (of4 *)buf(k, 1), (const of4 *)buf(k, 2), (const of4 *)buf(k, 3),
-                        (const float *)buf(k, 4), val_f(k, 5), val_f(k, 6), count);
+        (ref ? rscl_scat_sig_aux : or_scat_sig_aux)((of4 *)buf(k, 0), (of4 *)buf(k, 1), (const of4 *)buf(k, 2),
+                                                    (const of4 *)buf(k, 3), (const float *)buf(k, 4), val_f(k, 5),
+                                                    val_f(k, 6), count);
     } else if (!strcmp(n, "make_pulse_pass_1")) {
         const cl_uint range_count = val_u(k, 8), group_count = val_u(k, 9), items = val_u(k, 10);
         if (local == 0 || (size_t)group_count * range_count > buf_n16(k, 0)) return CL_INVALID_VALUE;
-        or_make_pulse_pass_1((of4 *)buf(k, 0), (const of4 *)buf(k, 1), (const of4 *)buf(k, 2), buf_n16(k, 1),
-                             (const float *)buf(k, 4), val_f(k, 5), *val_f(k, 6), *val_f(k, 7), range_count,
-                             group_count, items, (uint32_t)local);
+        (ref ? rscl_make_pulse_pass_1 : or_make_pulse_pass_1)(
+            (of4 *)buf(k, 0), (const of4 *)buf(k, 1), (const of4 *)buf(k, 2), buf_n16(k, 1), (const float *)buf(k, 4),
+            val_f(k, 5), *val_f(k, 6), *val_f(k, 7), range_count, group_count, items, (uint32_t)local);
     } else if (!strncmp(n, "make_pulse_pass_2_", 18)) {
         /* Pass 2 writes out[get_global_id(0)] for every work item, and its
          * global size is the launch plan's (rs.c:1355-1382), which can exceed
@@ -600,20 +621,32 @@ cl_int clEnqueueNDRangeKernel(cl_command_queue q, cl_kernel k, cl_uint dim, cons
         const size_t nout = buf_n16(k, 0) > count ? buf_n16(k, 0) : count;
         of4 *tmp = (of4 *)calloc(nout ? nout : 1, sizeof(of4));
         if (tmp == NULL) return CL_OUT_OF_HOST_MEMORY;
+        const of4 *in = (const of4 *)buf(k, 1);
+        const size_t in_n = buf_n16(k, 1);
         if (!strcmp(n, "make_pulse_pass_2_local")) {
-            or_make_pulse_pass_2_local_body(tmp, (const of4 *)buf(k, 1), buf_n16(k, 1), val_u(k, 3), val_u(k, 4),
-                                            count, local);
+            if (ref) {
+                rscl_make_pulse_pass_2_local(tmp, in, in_n, val_u(k, 3), val_u(k, 4), count, local);
+            } else {
+                or_make_pulse_pass_2_local_body(tmp, in, in_n, val_u(k, 3), val_u(k, 4), count, local);
+            }
         } else if (!strcmp(n, "make_pulse_pass_2_range")) {
-            or_make_pulse_pass_2_range_body(tmp, (const of4 *)buf(k, 1), buf_n16(k, 1), val_u(k, 3), val_u(k, 4),
-                                            count);
+            if (ref) {
+                rscl_make_pulse_pass_2_range(tmp, in, in_n, val_u(k, 3), val_u(k, 4), count, local);
+            } else {
+                or_make_pulse_pass_2_range_body(tmp, in, in_n, val_u(k, 3), val_u(k, 4), count);
+            }
         } else {
-            or_make_pulse_pass_2_group_body(tmp, (const of4 *)buf(k, 1), buf_n16(k, 1), val_u(k, 3), local);
+            if (ref) {
+                rscl_make_pulse_pass_2_group(tmp, in, in_n, val_u(k, 3), val_u(k, 4), count, local);
+            } else {
+                or_make_pulse_pass_2_group_body(tmp, in, in_n, val_u(k, 3), local);
+            }
         }
         memcpy(buf(k, 0), tmp, buf_n16(k, 0) * sizeof(of4));
         free(tmp);
     } else if (!strcmp(n, "pop")) {
         if (origin != 0 || count > buf_n16(k, 0)) return CL_INVALID_GLOBAL_OFFSET;
-        or_pop((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), val_f(k, 3), count);
+        (ref ? rscl_pop : or_pop)((of4 *)buf(k, 0), (of4 *)buf(k, 1), (of4 *)buf(k, 2), val_f(k, 3), count);
     } else {
         shim_error("kernel %s is not run by this device", n);
         return CL_INVALID_KERNEL;

@@ -38,6 +38,11 @@ typedef struct {
 } clshim_event;
 void clshim_set_hook(void (*hook)(const clshim_event *ev, void *user), void *user);
 
+/* The kernels the device runs: the oracle's restatement (the default) or the
+ * reference's own rs.cl compiled for the CPU (rscl.h). */
+enum { CLSHIM_KERNELS_ORACLE = 0, CLSHIM_KERNELS_RSCL = 1 };
+void clshim_set_kernels(int which);
+
 #ifdef __cplusplus
 }
 #endif

@@ -293,7 +293,8 @@ static void put_mem(const char *name, cl_mem m) {
 static void usage(void) {
     fprintf(stderr,
             "usage: refdrive OUT [--density D] [--scan S] [--pulses K] [--warmup W] [--seed N] [--concept BITS]\n"
-            "                    [--les CONFIG] [--debris TYPE:COUNT]... [--gate M] [--bundle DIR]\n");
+            "                    [--les CONFIG] [--debris TYPE:COUNT]... [--gate M] [--bundle DIR]\n"
+            "                    [--kernels oracle|rscl]\n");
     exit(2);
 }
 
@@ -318,7 +319,13 @@ int main(int argc, char **argv) {
         else if (!strcmp(argv[i], "--les") && i + 1 < argc) les = argv[++i];
         else if (!strcmp(argv[i], "--gate") && i + 1 < argc) gate = (float)atof(argv[++i]);
         else if (!strcmp(argv[i], "--bundle") && i + 1 < argc) bundle = argv[++i];
-        else if (!strcmp(argv[i], "--debris") && i + 1 < argc && ndeb < 8) {
+        else if (!strcmp(argv[i], "--kernels") && i + 1 < argc) {
+            /* oracle: the oracle's restatement; rscl: the reference's rs.cl */
+            const char *kk = argv[++i];
+            if (!strcmp(kk, "rscl")) clshim_set_kernels(CLSHIM_KERNELS_RSCL);
+            else if (!strcmp(kk, "oracle")) clshim_set_kernels(CLSHIM_KERNELS_ORACLE);
+            else usage();
+        } else if (!strcmp(argv[i], "--debris") && i + 1 < argc && ndeb < 8) {
             if (sscanf(argv[++i], "%d:%d", &deb_type[ndeb], &deb_count[ndeb]) != 2) usage();
             ndeb++;
         } else usage();
@@ -330,7 +337,8 @@ int main(int argc, char **argv) {
 
     /* simradar.c:796-955 */
     /* RS_init_verbose with the folder of rs_enum.h / rs.cl given (the shim
-     * reads the kernel source but runs the oracle's kernels) */
+     * reads the kernel source; it runs the oracle's kernels, or with
+     * --kernels rscl the reference's rs.cl compiled for the CPU) */
     H = RS_init_with_path(bundle, RS_METHOD_GPU, 0xFF, 0, 0);
     if (H == NULL) return 3;
     RS_set_concept(H, concept);

@@ -6,8 +6,10 @@ simradar_gb300 package.
 
 oracle/ref/Makefile compiles the reference's C modules unmodified from the
 reference tree (les.c, pos.c, adm.c, rcs.c, obj.c, log.c and rs.c, the last
-against this project's OpenCL shim over the CPU oracle).  They can be built
-only where the reference tree is present; `available()` says whether it is.
+against this project's OpenCL shim over the CPU oracle), and its kernel
+source rs.cl as C++ through oracle/ref/clc/opencl_c.hpp (`rscl()`).  They can
+be built only where the reference tree is present; `available()` says
+whether it is.
 """
 import ctypes
 import os
@@ -137,6 +139,54 @@ def les_descriptor(config):
     return desc
 
 
+# ------------------------------------------------- the reference's rs.cl
+class _RsclLib:
+    """The reference's rs.cl kernels compiled for the CPU (oracle/ref/rscl.h),
+    under the oracle's entry-point names: oracle.advance_time / db_rcs /
+    make_pulse(..., L=rscl()) run them where they would run the oracle's."""
+
+    def __init__(self, L, O):
+        self._L = L
+        img = O.Image
+        _s = ctypes.c_size_t
+        f32, u32, i32 = ctypes.c_float, ctypes.c_uint32, ctypes.c_int
+        sig = {
+            "el_atts": [_f, _f, _f, _u, img, _f, _f, _f, _f, _s, _s],
+            "bg_atts": [_f, _f, _f, _u, img, _f, _f, _f, _f, _s, _s],
+            "fp_atts": [_f, _f, _f, img, img, _f, _f, _s, _s],
+            "db_atts": [_f, _f, _f, _f, _f, _u, img, _f, img, img, _f, img, img, _f, _f, _f, _f, _s, _s],
+            "db_rcs": [_f, _f, _f, img, img, _f, _f, _s, _s],
+            "scat_sig_aux": [_f, _f, _f, _f, _f, _f, _f, _s],
+            "pop": [_f, _f, _f, _f, _s],
+            "make_pulse_pass_1": [_f, _f, _f, _s, _f, _f, f32, f32, u32, u32, u32, u32],
+            "make_pulse_pass_2_local": [_f, _f, _s, u32, u32, _s, _s],
+            "make_pulse_pass_2_range": [_f, _f, _s, u32, u32, _s, _s],
+            "make_pulse_pass_2_group": [_f, _f, _s, u32, u32, _s, _s],
+            "make_pulse": [_f, _f, _f, _f, _f, _s, _s, _f, _f, _f, _f, f32, f32, u32, _f, u32, u32, u32, i32],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, "rscl_" + name)
+            fn.argtypes = args
+            fn.restype = i32 if name == "make_pulse" else None
+
+    def __getattr__(self, name):
+        if name.startswith("or_"):
+            return getattr(self._L, "rscl_" + name[3:])
+        return getattr(self._L, name)
+
+
+_rscl = None
+
+
+def rscl():
+    """The reference's rs.cl kernels behind the oracle's entry-point names."""
+    global _rscl
+    if _rscl is None:
+        from . import oracle as O
+        _rscl = _RsclLib(lib(), O)
+    return _rscl
+
+
 # ---------------------------------------------------------------- sessions
 _DT = {"f4": np.float32, "u4": np.uint32, "i4": np.int32, "f8": np.float64, "u8": np.uint64}
 
@@ -182,12 +232,15 @@ def write_session(path, arrays):
 
 
 def run_session(out_path, home, density=0.3, pulses=20, warmup=130, debris=(), seed=19760520, gate=30.0,
-                scan="P:3.0,-12:12:0.24", concept=None, les="suctvort", threads=None):
-    """Run refdrive (rs.c on the oracle device) with the tables under
-    <home>/Documents/tables and return the record."""
+                scan="P:3.0,-12:12:0.24", concept=None, les="suctvort", threads=None, kernels="oracle"):
+    """Run refdrive (rs.c on the CPU device of the OpenCL shim) with the tables
+    under <home>/Documents/tables and return the record.  kernels: "oracle"
+    (the device runs the oracle's restatement of each rs.cl kernel) or "rscl"
+    (the reference's own rs.cl, compiled for the CPU)."""
     lib()
     cmd = [DRIVE, out_path, "--bundle", REFERENCE, "--density", repr(density), "--pulses", str(pulses),
-           "--warmup", str(warmup), "--seed", str(seed), "--gate", repr(gate), "--scan", scan, "--les", les]
+           "--warmup", str(warmup), "--seed", str(seed), "--gate", repr(gate), "--scan", scan, "--les", les,
+           "--kernels", kernels]
     if concept is not None:
         cmd += ["--concept", str(int(concept))]
     for t, n in debris:
