@@ -640,6 +640,14 @@ void or_make_pulse_pass_1(of4 *out, const of4 *sig, const of4 *aux, size_t n_all
     const float x0_0 = wd[1] + 0.0f;
     const float x0_1 = wd[1] + 1.0f;
     const float xm = wd[2];
+    /* the gate origins of every work item: range_start advanced by the
+     * kernel's repeated FP32 additions (rs.cl:1214), the same bits */
+    float *rk = (float *)malloc(sizeof(float) * (G ? G : 1));
+    float r = range_start;
+    for (uint32_t k = 0; k < G; k++) {
+        rk[k] = r;
+        r = r + range_delta;
+    }
 #pragma omp parallel for schedule(dynamic, 1)
     for (long long gg = 0; gg < (long long)group_count; gg++) {
         uint32_t group_id = (uint32_t)gg;
@@ -648,7 +656,13 @@ void or_make_pulse_pass_1(of4 *out, const of4 *sig, const of4 *aux, size_t n_all
          * it adds entries of the next gate's column, and for the last gate it
          * reads past the G x local_size array of the reference */
         of4 *shared = (of4 *)calloc((size_t)G * local_size + local_size, sizeof(of4));
+        /* one work item's G x 4 sums, gate-major: its entries of `shared`
+         * (shared[lid + k local_size]) receive the same additions in the same
+         * order from zero, so they are copied there when it is done; the gate
+         * loop then runs over contiguous memory */
+        float *acc = (float *)malloc(sizeof(float) * 4 * (G ? G : 1));
         for (uint32_t lid = 0; lid < local_size; lid++) {
+            memset(acc, 0, sizeof(float) * 4 * G);
             uint32_t i = group_id * group_stride + lid;
             while (i < n) {
                 uint32_t j = i + local_size;
@@ -656,29 +670,42 @@ void or_make_pulse_pass_1(of4 *out, const of4 *sig, const of4 *aux, size_t n_all
                 of4 s_b = ld_or_zero(sig, n_alloc, j);
                 of4 a_a = ld_or_zero(aux, n_alloc, i);
                 of4 a_b = ld_or_zero(aux, n_alloc, j);
-                float r_a = a_a.x, r_b = a_b.x;
-                float r = range_start;
-                s_a = f4(s_a.x * a_a.w, s_a.y * a_a.w, s_a.z * a_a.w, s_a.w * a_a.w);
-                s_b = f4(s_b.x * a_b.w, s_b.y * a_b.w, s_b.z * a_b.w, s_b.w * a_b.w);
+                const float r_a = a_a.x, r_b = a_b.x;
+                const float sax = s_a.x * a_a.w, say = s_a.y * a_a.w, saz = s_a.z * a_a.w, saw = s_a.w * a_a.w;
+                const float sbx = s_b.x * a_b.w, sby = s_b.y * a_b.w, sbz = s_b.z * a_b.w, sbw = s_b.w * a_b.w;
+                /* the four table coordinates of rs.cl's float4 fidx_raw
+                 * (r_a, r_a, r_b, r_b) - r, lane by lane */
+                const float x04[4] = {x0_0, x0_1, x0_0, x0_1};
                 for (uint32_t k = 0; k < G; k++) {
-                    float da = r_a - r, db = r_b - r;
-                    float f0, f1, f2, f3;
-                    float dec0 = cl_fract(cl_clamp(fmaf(da, xs, x0_0), 0.0f, xm), &f0);
-                    (void)cl_fract(cl_clamp(fmaf(da, xs, x0_1), 0.0f, xm), &f1);
-                    float dec2 = cl_fract(cl_clamp(fmaf(db, xs, x0_0), 0.0f, xm), &f2);
-                    (void)cl_fract(cl_clamp(fmaf(db, xs, x0_1), 0.0f, xm), &f3);
-                    float w_a = cl_mix(W[cl_f2u_rtz(f0)], W[cl_f2u_rtz(f1)], dec0);
-                    float w_b = cl_mix(W[cl_f2u_rtz(f2)], W[cl_f2u_rtz(f3)], dec2);
-                    of4 *sh = &shared[lid + (size_t)k * local_size];
-                    sh->x = sh->x + (w_a * s_a.x + w_b * s_b.x);
-                    sh->y = sh->y + (w_a * s_a.y + w_b * s_b.y);
-                    sh->z = sh->z + (w_a * s_a.z + w_b * s_b.z);
-                    sh->w = sh->w + (w_a * s_a.w + w_b * s_b.w);
-                    r = r + range_delta;
+                    const float d4[4] = {r_a - rk[k], r_a - rk[k], r_b - rk[k], r_b - rk[k]};
+                    float fl[4], dec[4], w[4];
+                    for (int l = 0; l < 4; l++) {
+                        const float v = cl_clamp(fmaf(d4[l], xs, x04[l]), 0.0f, xm);
+                        fl[l] = floorf(v);
+                        dec[l] = fminf(v - fl[l], 0x1.fffffep-1f);   /* fract */
+                    }
+                    /* the indices are floors of values clamped to [0, xm]: in
+                     * range, so the conversion is convert_uint's */
+                    for (int l = 0; l < 4; l++) w[l] = W[(uint32_t)fl[l]];
+                    const float w_a = cl_mix(w[0], w[1], dec[0]);
+                    const float w_b = cl_mix(w[2], w[3], dec[2]);
+                    float *a = acc + 4 * k;
+                    a[0] = a[0] + (w_a * sax + w_b * sbx);
+                    a[1] = a[1] + (w_a * say + w_b * sby);
+                    a[2] = a[2] + (w_a * saz + w_b * sbz);
+                    a[3] = a[3] + (w_a * saw + w_b * sbw);
                 }
                 i += local_stride;
             }
+            for (uint32_t k = 0; k < G; k++) {
+                of4 *sh = &shared[lid + (size_t)k * local_size];
+                sh->x = acc[4 * k];
+                sh->y = acc[4 * k + 1];
+                sh->z = acc[4 * k + 2];
+                sh->w = acc[4 * k + 3];
+            }
         }
+        free(acc);
         /* the log-step tree of rs.cl:1224-1290 */
         const uint32_t local_numel = G * local_size;
         for (uint32_t half = 512; half >= 1; half >>= 1) {
@@ -701,6 +728,7 @@ void or_make_pulse_pass_1(of4 *out, const of4 *sig, const of4 *aux, size_t n_all
         }
         free(shared);
     }
+    free(rk);
 }
 
 /* ---- make_pulse_pass_2_local body (rs.cl:1304-1338) ---- */
