@@ -108,6 +108,29 @@ def test_advance_kernels_match_rs_cl(rscl, concept):
         assert respawned[:S.counts[0]].sum() >= 64 and respawned[S.counts[0]:].sum() >= 16
 
 
+def test_uniform_les_grid_matches_rs_cl(rscl):
+    """wind_table_index's uniform branch (rs.cl:152-173: fma(pos, scale,
+    origin)) with the LES volume spread over the scan box, el_atts and
+    db_atts."""
+    S = synth.make_scene(num_rain=8000, debris=[(synth.OBJ_LEAF, 300), (synth.OBJ_BRICK, 300)], les_count=1)
+    push_to_edges(S)
+    ox, oy, oz, sx, sy, sz = S.box
+    n = (S.les_cfg.nx, S.les_cfg.ny, S.les_cfg.nz)
+    desc = np.zeros(16, np.float32)   # spacing code 0 (uniform) in lane 7
+    for ax, (o, size) in enumerate(((ox, sx), (oy, sy), (oz, sz))):
+        desc[ax] = np.float32(n[ax] / size)
+        desc[4 + ax] = np.float32(-o * n[ax] / size)
+    desc[3] = S.les_desc[3]
+    S.les_desc = desc
+    a, b = O.OracleState(S.state), O.OracleState(S.state)
+    for k in range(4):
+        sd = concept_desc(S, k, synth.CONCEPT_DBU)
+        O.advance_time(a, S, S.counts, S.les[0], sd)
+        O.advance_time(b, S, S.counts, S.les[0], sd, L=rscl)
+        assert_advance_equal(a, b, S.counts[0], "uniform LES step %d" % k)
+    assert not np.array_equal(bits(a.s["vel"]), bits(S.state["vel"]))
+
+
 @pytest.mark.parametrize("mode", [0.0, 1.0, 2.0])
 def test_debris_flux_field_matches_rs_cl(rscl, mode):
     """db_atts's respawn from the debris flux field (rs.cl:795-835): plain,
