@@ -38,6 +38,10 @@ Extra sections on one GPU (added to the same JSON line):
              host buffers every 100 pulses and on to a .iq file by the
              backend's background writer, one LES slot refilled on the copy
              stream during the run.
+  small      the reference's CPU-runnable case: 131,072 rain (DBU), the
+             same PPI, 100 pulses -- on the GPU through the C ABI (every
+             pulse copied back) and on the host cores with the oracle after
+             one warm pulse.
 """
 import argparse
 import json
@@ -59,7 +63,7 @@ DEBRIS = ((1, 1024), (3, 1024), (6, 1024))
 GATES = 40
 METRIC = "pulses/s and scatterer-updates/s at 2M scatterers; HBM roofline frac; I/Q err vs FP64"
 UNIT = "pulses/s"
-SECTIONS = ("precision", "batch", "les", "large")
+SECTIONS = ("precision", "batch", "les", "large", "small")
 SORT_INTERVAL = 128   # the backend's default (rsc_set_sort_interval)
 
 
@@ -658,6 +662,41 @@ def bench_les(torch, rsc, synth, dev, S, steps=2000, period=100, repeats=3):
             "h2d_bytes_per_swap_blocking": nn * 32, "h2d_bytes_per_swap_source": nn * 20}
 
 
+def bench_small(torch, rsc, synth, dev, pulses=100):
+    """The reference's CPU-runnable configuration: 131,072 rain scatterers
+    (concept DBU), PPI 3.0 deg, -12..12 deg at 0.24 deg, 40 gates at 15 m,
+    100 pulses.  GPU: the pulses through the C ABI with every pulse copied to
+    pinned host memory (host clock, after three warm pulses).  CPU: the
+    oracle (every host core) on the same 100 pulses after one warm pulse."""
+    S = synth.make_scene(num_rain=131072, gates=GATES, les_count=1)
+    S.sd_seq = [synth.pulse_sim_desc(S, k, tic=k * 1e-3) for k in range(len(S.scan))]
+    pop = synth.population(S)
+    W = rsc.Worker(dev)
+    synth.load_worker(W, S)
+    ring = torch.empty((pulses, GATES, 4), dtype=torch.float32).pin_memory()
+    ring_np = ring.numpy()
+    for k in range(3):
+        W.make_pulse(S.sd_seq[k])
+        W.advance_time(pop, 0, S.sd_seq[k])
+    W.synchronize()
+    t0 = time.perf_counter()
+    for k in range(pulses):
+        sd = S.sd_seq[k % len(S.sd_seq)]
+        W.make_pulse(sd)
+        W.download_pulse_async(ring_np[k])
+        W.advance_time(pop, 0, sd)
+    W.synchronize()
+    gpu_s = time.perf_counter() - t0
+    W.close()
+    cpu_value, cores = cpu_reference(S, pulses=pulses, warm=1)
+    return {"workload": "131,072 rain, concept DBU, PPI 3.0 deg -12..12 deg / 0.24 deg, %d gates @ 15 m, "
+                        "%d pulses" % (GATES, pulses),
+            "gpu_pulses_per_s": pulses / gpu_s, "cpu_pulses_per_s": cpu_value, "cpu_cores": cores,
+            "cpu": cpu_model(), "gpu_over_cpu": (pulses / gpu_s) / cpu_value,
+            "note": "GPU through the C ABI with every pulse copied to pinned host memory (host clock); CPU: "
+                    "the oracle on the same pulses after one warm pulse"}
+
+
 def run_ours(args, rank, world):
     from simradar_gb300 import build as Bld
     from simradar_gb300 import rsc, synth
@@ -803,6 +842,8 @@ def run_ours(args, rank, world):
             extras["les"] = bench_les(torch, rsc, synth, dev, S)
         if "large" in wanted:
             extras["large"] = bench_large(torch, rsc, synth, dev, chunks=100)
+        if "small" in wanted and not args.no_cpu_baseline:
+            extras["small"] = bench_small(torch, rsc, synth, dev)
 
     # CPU baseline: the oracle on a bounded sample of the same workload
     cpu = None
