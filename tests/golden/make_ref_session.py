@@ -12,6 +12,8 @@ absent.  Each fixture holds what rs.c derived and sent to the device (tables,
 descriptors, population layout, the event list with every descriptor), the
 pulses it read back, and hashes of the uploaded state, of every LES frame
 and of the final state (tests/test_ref_session.py, tests/test_gpu_ref_session.py).
+ref_session_dbu_rscl is the DBU session with the device running the
+reference's own rs.cl kernels rather than the oracle's.
 
     python tests/golden/make_ref_session.py [session ...]
 """
@@ -47,6 +49,10 @@ SESSIONS = {
     "ref_session_vpr": dict(density=0.3, pulses=24, warmup=60, seed=97531, gate=30.0,
                             scan="P:90.0,0:360:1.0", concept=90, debris=[(synth.OBJ_LEAF, 128)]),
 }
+# The same DBU session with the shim's device running the reference's own
+# rs.cl (compiled for the CPU through oracle/ref/clc/opencl_c.hpp) instead of
+# the oracle's restatement of its kernels.
+SESSIONS["ref_session_dbu_rscl"] = dict(SESSIONS["ref_session_dbu"], kernels="rscl")
 TABLES = dict(seed=7, volumes_per_file=10, adm_dims=(37, 19), rcs_dims=(37, 19))
 
 
@@ -60,7 +66,7 @@ def record(name, home, work):
     if int(R["failed"]):
         raise RuntimeError("refdrive reported failed checks for " + name)
     meta = {"density": args["density"], "pulses": args["pulses"], "warmup": args["warmup"], "gate": args["gate"],
-            "scan": args["scan"], "concept": args["concept"],
+            "scan": args["scan"], "concept": args["concept"], "kernels": args.get("kernels", "oracle"),
             "debris": np.array(args["debris"], np.int64).reshape(-1, 2),
             "tables_seed": TABLES["seed"], "tables_volumes_per_file": TABLES["volumes_per_file"],
             "tables_adm_dims": np.array(TABLES["adm_dims"]), "tables_rcs_dims": np.array(TABLES["rcs_dims"])}

@@ -12,7 +12,10 @@ against the recording:
 
   * the LES descriptor bit for bit, every LES frame read (hash), the state
     after populate (hash);
-  * the final state -- pos, vel, ori, tum, aux, rcs, sig, rnd -- bit for bit;
+  * the final state -- pos, vel, ori, tum, aux, rcs, sig, rnd -- bit for bit
+    (ref_session_dbu_rscl, recorded with the device running the reference's
+    own rs.cl: bit for bit but for the rain backscatter and the signals
+    formed from it, within 4e-7);
   * every pulse read back within 2e-5 of the per-gate sum of |term| against
     both the pulse rs.c read back and the exact sum of its terms, and the
     merged, scaled pulse with the gain of RS_merge_pulse_tmp.
@@ -26,7 +29,7 @@ import pytest
 from oracle import refbind
 from simradar_gb300 import build as B
 
-from test_ref_session import FIELDS, SESSIONS, load, write_session_tables
+from test_ref_session import ALL_SESSIONS, FIELDS, SESSIONS, SESSIONS_RSCL, load, write_session_tables
 
 pytestmark = pytest.mark.gpu
 
@@ -54,7 +57,7 @@ def bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-@pytest.mark.parametrize("name", SESSIONS)
+@pytest.mark.parametrize("name", ALL_SESSIONS)
 def test_c_host_replays_rs_c_session(name, host_loop, tables, tmp_path):
     R = load(name)
     sess = str(tmp_path / "session.bin")
@@ -78,9 +81,18 @@ def test_c_host_replays_rs_c_session(name, host_loop, tables, tmp_path):
     gain = float(np.abs(R["pulse_merged"]).max() / max(np.abs(R["pulse_raw"]).max(), 1e-30))
     err = np.abs(O["pulse_merged"].astype(np.float64) - R["pulse_merged"].astype(np.float64))
     assert np.all(err <= 2e-5 * ab * gain * 1.0001 + 1e-30)
-    # the final state, bit for bit
+    # the final state, bit for bit; against a session run on the reference's
+    # own rs.cl, the rain backscatter (|xy|^2 / |xyz|^2 here, cos(atan2)^2
+    # there) and the signals formed from it within 4e-7
+    near = ("rcs", "sig") if name in SESSIONS_RSCL else ()
     bad = []
     for i, f in enumerate(FIELDS):
+        if f in near:
+            x = R["final_%s_every8" % f].astype(np.float64)
+            y = O["final_%s_every8" % f].astype(np.float64)
+            if not np.all(np.abs(x - y) <= 4e-7 * np.abs(x)):
+                bad.append("%s beyond 4e-7" % f)
+            continue
         if int(O["final_hash"][i]) != int(R["final_hash"][i]):
             g, r = O["final_%s_every8" % f].view(np.uint32), R["final_%s_every8" % f].view(np.uint32)
             rows = np.nonzero((g != r).any(axis=1))[0]

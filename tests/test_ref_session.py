@@ -13,6 +13,9 @@ These CPU tests check against those recordings:
     every GPU parity test) replays rs.c's event list to the same pulses and
     the same final state, bit for bit (with the debris flux field tables rs.c
     derived from each LES frame in the session with that concept);
+  * for ref_session_dbu_rscl, recorded with the device running the
+    reference's own rs.cl, that the replay gives the same final state bit
+    for bit but for the rain backscatter and the signals formed from it;
   * where the reference tree is present, that the recording is reproduced.
 """
 import math
@@ -28,6 +31,9 @@ from simradar_gb300 import rsc, synth
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 SESSIONS = ["ref_session_dbu", "ref_session_bg", "ref_session_dff", "ref_session_vpr"]
+# recorded with the device running the reference's own rs.cl kernels
+SESSIONS_RSCL = ["ref_session_dbu_rscl"]
+ALL_SESSIONS = SESSIONS + SESSIONS_RSCL
 FIELDS = ["pos", "vel", "ori", "tum", "aux", "rcs", "sig", "rnd"]
 EV_LES, EV_ADVANCE, EV_DEBRIS_RCS, EV_PULSE, EV_UPLOAD = 1, 2, 3, 4, 5
 
@@ -86,7 +92,7 @@ def tables_home(tmp_path_factory):
     return home, les_dir
 
 
-@pytest.mark.parametrize("name", SESSIONS)
+@pytest.mark.parametrize("name", ALL_SESSIONS)
 def test_recording_is_consistent(name):
     R = load(name)
     assert int(R["failed"]) == 0 and int(R["uploads"]) == 1
@@ -104,7 +110,7 @@ def test_recording_is_consistent(name):
     np.testing.assert_allclose(R["pulse_merged"], R["pulse_raw"] * gain, rtol=2e-6, atol=0)
 
 
-@pytest.mark.parametrize("name", SESSIONS)
+@pytest.mark.parametrize("name", ALL_SESSIONS)
 def test_populate_is_rs_populate(name):
     """rsc_populate_host (the backend's RS_populate) against the state rs.c
     uploaded, bit for bit."""
@@ -115,7 +121,7 @@ def test_populate_is_rs_populate(name):
     assert np.array_equal(pop.astype(np.uint64), R["dsd_pop"])
 
 
-@pytest.mark.parametrize("name", SESSIONS)
+@pytest.mark.parametrize("name", ALL_SESSIONS)
 def test_host_tables_match_synth(name):
     """The tables and descriptors the tests and the bench build with synth
     against the ones rs.c made for the same radar."""
@@ -149,7 +155,7 @@ def test_host_tables_match_synth(name):
         assert np.array_equal(bits(rd), bits(R["rcs_desc_%d" % r]))
 
 
-@pytest.mark.parametrize("name", SESSIONS)
+@pytest.mark.parametrize("name", ALL_SESSIONS)
 def test_beam_positions_match(name):
     """The beam unit vector of every pulse descriptor against synth's
     RS_set_beam_pos of the scan's positions.  Loop pulse k sees position k:
@@ -217,8 +223,42 @@ def test_oracle_replays_rs_c(name, tables_home):
         assert np.array_equal(st.s[f][::8].view(np.uint32), R["final_%s_every8" % f].view(np.uint32)), f
 
 
+def assert_state_near_rs_cl(st_s, R):
+    """The final state against a session run on rs.cl: bit for bit but for
+    the rain backscatter (the oracle's cos^2 of the elevation is
+    |xy|^2 / |xyz|^2, rs.cl's cos(atan2(z, |xy|))^2) and the signals formed
+    from it, which agree within 4e-7 relative."""
+    for i, f in enumerate(FIELDS):
+        if f in ("rcs", "sig"):
+            x = R["final_%s_every8" % f].astype(np.float64)
+            y = st_s[f][::8].astype(np.float64)
+            assert np.all(np.abs(x - y) <= 4e-7 * np.abs(x)), f
+        else:
+            assert refbind.fnv1a(st_s[f]) == int(R["final_hash"][i]), f
+
+
+def assert_pulses_near(got, R):
+    """Pulses within 2e-5 of the per-gate sum of |term| of the recording."""
+    ab = R["pulse_abs"].astype(np.float64)
+    err = np.abs(got.astype(np.float64) - R["pulse_raw"].astype(np.float64))
+    assert np.all(err <= 2e-5 * ab + 1e-30), float((err / (ab + 1e-30)).max())
+
+
+@pytest.mark.parametrize("name", SESSIONS_RSCL)
+def test_oracle_replays_rs_cl_session(name, tables_home):
+    """rs.c's session run with the reference's own rs.cl kernels, replayed by
+    the oracle's Python orchestration: the same final positions, velocities,
+    orientations, tumbles, aux and seeds, bit for bit."""
+    R = load(name)
+    assert str(R["meta_kernels"]) == "rscl"
+    _, les_dir = tables_home
+    pulses, st = replay_oracle(R, les_dir)
+    assert_pulses_near(pulses, R)
+    assert_state_near_rs_cl(st.s, R)
+
+
 @pytest.mark.skipif(not refbind.available(), reason="the reference tree is not present")
-@pytest.mark.parametrize("name", SESSIONS)
+@pytest.mark.parametrize("name", ALL_SESSIONS)
 def test_recording_reproduces(name, tables_home, tmp_path):
     """rs.c run again gives the recorded session (the oracle sums of |term|
     are per-thread double sums: compared to 1e-12)."""
