@@ -513,11 +513,15 @@ __device__ __forceinline__ float range_weight(const PulseArgs &P, float d) {
  * 1 - (x0 - 1); at x0 = 2 it is 0.  The GPU test of rsc_eval_math function
  * 8 compares it with the oracle's table lerp around every breakpoint. */
 __device__ __forceinline__ float range_weight_tri(const float *rwd, float d) {
-    const float x0 = cl_clamp(fmaf(d, rwd[0], rwd[1] + 0.0f), 0.0f, 2.0f);
-    const float x1 = cl_clamp(fmaf(d, rwd[0], rwd[1] + 1.0f), 0.0f, 2.0f);
-    const float up = x1 < 2.0f ? x0 : 0.0f;
-    const float down = x0 < 2.0f ? 1.0f - (x0 - 1.0f) : 0.0f;
-    return x0 < 1.0f ? up : down;
+    /* t0, t1: the two raw indices; their clamps to [0, 2] are not formed.
+     * On the rising side (t0 < 1) x0 = clamp(t0) is max(t0, 0) and x1 < 2
+     * is t1 < 2; on the falling side x0 < 2 is t0 < 2, where x0 = t0.  A NaN
+     * index gives 0, as the clamped form does. */
+    const float t0 = fmaf(d, rwd[0], rwd[1] + 0.0f);
+    const float t1 = fmaf(d, rwd[0], rwd[1] + 1.0f);
+    const float up = t1 < 2.0f ? fmaxf(t0, 0.0f) : 0.0f;
+    const float down = t0 < 2.0f ? 1.0f - (t0 - 1.0f) : 0.0f;
+    return t0 < 1.0f ? up : down;
 }
 
 /* the same weight with a table of at most 4 entries held in the kernel

@@ -1017,12 +1017,14 @@ struct PulseBins {
 #pragma unroll
                 for (int q = 0; q < K; q++) {
                     float w = 0.0f;
-                    if (gate >= klo[q] && gate <= khi[q]) {
-                        if constexpr (TRI == 1) {
-                            w = range_weight_tri(P.rwd, rr[q] - rkj);
-                        } else {
-                            w = range_weight_reg(P, rr[q] - rkj);
-                        }
+                    if constexpr (TRI == 1) {
+                        /* every gate of the warp's window: outside the
+                         * lane's own candidate gates the triangle gives 0,
+                         * and 0 x c adds nothing to the sums, so the
+                         * per-gate test is left out */
+                        w = range_weight_tri(P.rwd, rr[q] - rkj);
+                    } else if (gate >= klo[q] && gate <= khi[q]) {
+                        w = range_weight_reg(P, rr[q] - rkj);
                     }
                     /* fused: the lane's K terms of a gate in one rounding each */
                     v0 = fmaf(w, c[q][0], v0);
