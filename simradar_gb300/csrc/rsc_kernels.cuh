@@ -509,8 +509,8 @@ __device__ __forceinline__ float range_weight(const PulseArgs &P, float d) {
  * on the rising side (index x0 in [0, 1)) the mix is 0 + (1 - 0) x0 = x0,
  * unless the second index has already rounded up to the last entry (x1 = 2,
  * a rounding corner within 2^-24 of the peak), where both picks are 0; on
- * the falling side (x0 in [1, 2)) it is 1 + (0 - 1)(x0 - 1), one rounding of
- * 1 - (x0 - 1); at x0 = 2 it is 0.  The GPU test of rsc_eval_math function
+ * the falling side (x0 in [1, 2)) it is 1 + (0 - 1)(x0 - 1) = 1 - (x0 - 1),
+ * which is exact there; at x0 = 2 it is 0.  The GPU test of rsc_eval_math function
  * 8 compares it with the oracle's table lerp around every breakpoint. */
 __device__ __forceinline__ float range_weight_tri(const float *rwd, float d) {
     /* t0, t1: the two raw indices; their clamps to [0, 2] are not formed.
@@ -520,7 +520,10 @@ __device__ __forceinline__ float range_weight_tri(const float *rwd, float d) {
     const float t0 = fmaf(d, rwd[0], rwd[1] + 0.0f);
     const float t1 = fmaf(d, rwd[0], rwd[1] + 1.0f);
     const float up = t1 < 2.0f ? fmaxf(t0, 0.0f) : 0.0f;
-    const float down = t0 < 2.0f ? 1.0f - (t0 - 1.0f) : 0.0f;
+    /* on [1, 2) both t0 - 1 and 1 - (t0 - 1) are exact (Sterbenz; a
+     * multiple of 2^-23 in (0, 1]), so the falling side is 2 - t0, and
+     * max(2 - t0, 0) gives the 0 at and beyond 2 (NaN: 0) */
+    const float down = fmaxf(2.0f - t0, 0.0f);
     return t0 < 1.0f ? up : down;
 }
 

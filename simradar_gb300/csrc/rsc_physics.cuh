@@ -96,10 +96,11 @@ __device__ __forceinline__ void tex_axis(float u, int n, int *i0, int *i1, float
     float uu = u - 0.5f;
     float fl = floorf(uu);
     *a = uu - fl;
-    float flc = fminf(fmaxf(fl, -1.0f), (float)n);
-    int i = (int)flc;
-    *i0 = min(max(i, 0), n - 1);
-    *i1 = min(max(i + 1, 0), n - 1);
+    /* the texel pair clamp(i), clamp(i + 1) to [0, n - 1]: with i first
+     * clamped to [-1, n - 1] (NaN -> -1) only one side of each can go out */
+    int i = (int)fminf(fmaxf(fl, -1.0f), (float)(n - 1));
+    *i0 = max(i, 0);
+    *i1 = min(i + 1, n - 1);
 }
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
