@@ -251,7 +251,9 @@ __device__ __forceinline__ float4 compute_dudt_dwdt(float4 *dwdt, float4 vel, fl
 /* compute_ellipsoid_rcs (rs.cl:268-280) */
 __device__ __forceinline__ float4 compute_ellipsoid_rcs(float4 pos, const float4 *table, const float *td) {
     float fidx = cl_clamp(fmaf(pos.w, td[0], td[1]), 0.0f, td[2]);
-    uint32_t idx = cl_f2u_rtz(fidx);
+    /* clamped to [0, td[2]] (NaN -> 0), inside the table: the plain
+     * truncating conversion is convert_uint's */
+    uint32_t idx = (uint32_t)fidx;
     float4 xz = ldg4(table + idx);
     /* cos^2 of the elevation beta = atan2(z, |xy|), formed as |xy|^2 / |xyz|^2:
      * the same quantity as cos(beta) * cos(beta) without the two
