@@ -595,6 +595,22 @@ int moment_span(const PulseArgs &P) {
     return (int)n;
 }
 
+
+/* The margin, in gates, by which the sparse path widens the exact support
+ * d_lo .. d_hi (metres) of the range weight: the measured drift of the FP32
+ * running-sum gate origins from exact spacing; two ulps of the largest range
+ * a window can reach (the rounding of r - r0 and of the gate origins there);
+ * and a few FP32 roundings of g = (r - r0) / delta, of the window bounds and
+ * of the weight's raw index, relative to the gate span, with a floor of 1e-4
+ * gate.  A gate outside the widened window gets an exactly zero weight. */
+double window_margin(double drift, float range_start, float range_delta, uint32_t G, double d_lo, double d_hi) {
+    const double delta = (double)range_delta;
+    const double span = (double)G + (fabs(d_lo) + fabs(d_hi)) / delta + 2.0;
+    const double r_max = fabs((double)range_start) + delta * span;
+    const double ulp_r = ldexp(1.0, ilogb(r_max) - 23);
+    return (drift + 2.0 * ulp_r) / delta + 8.0 * ldexp(1.0, -23) * span + 1.0e-4;
+}
+
 void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
     memset(&P, 0, sizeof(P));
     P.pos = w->pos;
@@ -642,7 +658,7 @@ void fill_pulse_args(rsc_worker *w, PulseArgs &P, const float *sim) {
                 rf = rf + w->range_delta;
                 r += (double)w->range_delta;
             }
-            double margin = (drift + 1.0e-3 * fabs((double)w->range_delta)) / (double)w->range_delta + 0.05;
+            const double margin = window_margin(drift, w->range_start, w->range_delta, w->G, d_lo, d_hi);
             double lo = d_lo / (double)w->range_delta - margin;
             double hi = d_hi / (double)w->range_delta + margin;
             if (hi - lo + 1.0 < (double)rsc::kMaxCandidates) {
@@ -3024,7 +3040,7 @@ int rsc_make_pulse_noalloc(const float *pos4, const float *rcs4, size_t num_scat
             drift = fmax(drift, fabs((double)rf - ((double)range_start + (double)k * (double)range_delta)));
             rf = rf + range_delta;
         }
-        double margin = (drift + 1.0e-3 * fabs((double)range_delta)) / (double)range_delta + 0.05;
+        const double margin = window_margin(drift, range_start, range_delta, G, d_lo, d_hi);
         double lo = d_lo / (double)range_delta - margin, hi = d_hi / (double)range_delta + margin;
         if (hi - lo + 1.0 < (double)rsc::kMaxCandidates) {
             P.dense = 0;
