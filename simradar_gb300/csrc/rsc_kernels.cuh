@@ -129,7 +129,7 @@ __device__ __forceinline__ void rain_el_next(const AdvanceArgs &a, size_t i, Rai
         vel.y = vel.y + dudt.y * dt;
         vel.z = vel.z + dudt.z * dt;
         vel.w = vel.w + dudt.w * 0.0f;
-        if ((concept & kConceptBounded) && len4(vel) > fmaxf(1.0f, 3.0f * len4(bg_vel))) {
+        if ((concept & kConceptBounded) && len4_exceeds_bound(vel, bg_vel)) {
             vel.x = bg_vel.x + 0.0f * dt;
             vel.y = bg_vel.y + 0.0f * dt;
             vel.z = bg_vel.z + g_dt;

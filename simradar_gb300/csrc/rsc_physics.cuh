@@ -64,6 +64,18 @@ __device__ __forceinline__ uint32_t cl_f2u_rtz(float f) {
 }
 __device__ __forceinline__ float len3(float x, float y, float z) { return sqrtf(x * x + y * y + z * z); }
 __device__ __forceinline__ float len4(float4 v) { return sqrtf(v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w); }
+/* len4(v) > max(1, 3 len4(b)) (el_atts' bound on the drop's velocity,
+ * rs.cl:714), decided as those FP32 operations decide it.  When the squared
+ * lengths are 0.1% or more below the squared bound -- far beyond the few
+ * roundings between them and the two lengths -- the answer is false without
+ * the square roots; otherwise (and for NaN or infinite lengths) the
+ * reference's operations decide. */
+__device__ __forceinline__ bool len4_exceeds_bound(float4 v, float4 b) {
+    const float a2 = v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w;
+    const float b2 = b.x * b.x + b.y * b.y + b.z * b.z + b.w * b.w;
+    if (a2 < 0.999f * fmaxf(1.0f, 9.0f * b2)) return false;
+    return sqrtf(a2) > fmaxf(1.0f, 3.0f * sqrtf(b2));
+}
 __device__ __forceinline__ float4 normalize4(float4 v) {
     float l = len4(v);
     return f4(v.x / l, v.y / l, v.z / l, v.w / l);
