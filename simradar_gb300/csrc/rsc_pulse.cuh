@@ -498,6 +498,17 @@ __device__ __forceinline__ bool warp_coherent(bool has, int k_lo, int k_hi, int 
     return w_hi - w_lo < span;
 }
 
+/* x = fma(w, a, x) and y = fma(w, b, y), each rounded once as fmaf rounds
+ * it: one packed FP32 instruction (fma.rn.f32x2) for the two */
+__device__ __forceinline__ void fma_pair(float w, float a, float b, float &x, float &y) {
+    unsigned long long wp, ab, xy;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(wp) : "f"(w));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ab) : "f"(a), "f"(b));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(xy) : "f"(x), "f"(y));
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(xy) : "l"(wp), "l"(ab));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(xy));
+}
+
 /* Add the warp's sum of four values into bin[0..3]: a transposed butterfly
  * (6 shuffles instead of 20) leaves the sum of value c in lanes 8c..8c+7,
  * and lanes 0, 8, 16, 24 add them to the warp's own bins (no other warp
@@ -1027,10 +1038,8 @@ struct PulseBins {
                         w = range_weight_reg(P, rr[q] - rkj);
                     }
                     /* fused: the lane's K terms of a gate in one rounding each */
-                    v0 = fmaf(w, c[q][0], v0);
-                    v1 = fmaf(w, c[q][1], v1);
-                    v2 = fmaf(w, c[q][2], v2);
-                    v3 = fmaf(w, c[q][3], v3);
+                    fma_pair(w, c[q][0], c[q][1], v0, v1);
+                    fma_pair(w, c[q][2], c[q][3], v2, v3);
                 }
                 warp_reduce4_add(fbins + (size_t)gate * kBinStride32, lane, v0, v1, v2, v3);
             }
