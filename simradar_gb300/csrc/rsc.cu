@@ -595,7 +595,6 @@ int moment_span(const PulseArgs &P) {
     return (int)n;
 }
 
-
 /* The margin, in gates, by which the sparse path widens the exact support
  * d_lo .. d_hi (metres) of the range weight: the measured drift of the FP32
  * running-sum gate origins from exact spacing; two ulps of the largest range
